@@ -1,0 +1,217 @@
+/*
+ * subway_gb300.h — C ABI of the GB300-native out-of-HBM graph engine.
+ *
+ * This is the drop-in boundary for Subway's hot path: graph loading, the
+ * per-iteration subgraph generation (activeness -> scan -> compaction ->
+ * active-edge gather), partitioned host->device transfer under a device-memory
+ * budget, and the BFS/SSSP/SSWP/CC/PR relaxation kernels in sync and async
+ * variants.  Every entry point is plain C: pointers and sizes, no C++ or torch
+ * types.  Every function returns an int status (SGW_OK = 0, negative = error)
+ * and never exits the process; the reference calls exit() from inside library
+ * code (shared/gpu_error_check.cuh:9-15, shared/graph.cu:171-175,
+ * shared/partitioner.cu:66-70).
+ *
+ * Paths in the citations are relative to the Subway source tree.
+ */
+#ifndef SUBWAY_GB300_H
+#define SUBWAY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SGW_OK          0
+#define SGW_EINVAL     -1   /* bad argument                                  */
+#define SGW_EIO        -2   /* file could not be opened / read / written     */
+#define SGW_EFORMAT    -3   /* unsupported extension or malformed file       */
+#define SGW_ENOMEM     -4   /* host allocation failed                        */
+#define SGW_EBUDGET    -5   /* device budget too small for the vertex state  */
+#define SGW_ECUDA      -6   /* a CUDA runtime call failed                    */
+#define SGW_ETIMEOUT   -7   /* a bounded device-side wait gave up            */
+#define SGW_ESTATE     -8   /* call made in the wrong engine state           */
+#define SGW_ERANGE     -9   /* size beyond a documented limit                */
+
+/* ---- algorithms and modes (subway/{bfs,sssp,sswp,cc,pr}-{sync,async}.cu) */
+#define SGW_BFS   0
+#define SGW_SSSP  1
+#define SGW_SSWP  2
+#define SGW_CC    3
+#define SGW_PR    4
+#define SGW_SYNC  0
+#define SGW_ASYNC 1
+
+/* DIST_INFINITY = UINT_MAX - 1 (shared/globals.hpp:27). */
+#define SGW_DIST_INFINITY 4294967294u
+
+typedef struct sgw_graph sgw_graph;
+typedef struct sgw_engine sgw_engine;
+
+/* Human-readable text for a status code, and the message of the last error
+ * raised on the calling thread (empty string if none). */
+const char *sgw_strerror(int status);
+const char *sgw_last_error(void);
+
+/* ---- graph (host side) --------------------------------------------------
+ * The on-disk and in-memory edge records are the reference's:
+ * OutEdge {u32 end} (4 B) and OutEdgeWeighted {u32 end; u32 w8} (8 B)
+ * (shared/globals.hpp:33-40).  Binary CSR files are
+ * [u32 n][u32 m][u32 nodePointer x n][edge x m]
+ * (shared/graph.cu:39-52, tools/converter.cpp:88-95).                       */
+
+/* Replaces Graph<E>::ReadGraph / GraphPR<E>::ReadGraph
+ * (shared/graph.cu:32-197, :229-394).  The type is chosen by the extension:
+ * .bcsr/.el unweighted, .bwcsr/.wel weighted (shared/graph.cu:37-53).
+ * out-degree is derived for every vertex (the reference leaves
+ * outDegree[n-2] unset, shared/graph.cu:179-181). */
+int sgw_graph_load(const char *path, sgw_graph **out);
+
+/* Wraps a caller-owned host CSR without copying it.  node_pointer has n+1
+ * entries (node_pointer[n] == m); edges holds m records of 4 B (weighted=0)
+ * or 8 B (weighted=1).  The arrays must outlive the graph object and every
+ * engine created on it.  Counterpart of the arrays that
+ * Graph<E>::ReadGraph fills (shared/graph.cu:46-51). */
+int sgw_graph_from_csr(uint32_t n, uint32_t m, const uint32_t *node_pointer,
+                       const void *edges, int weighted, sgw_graph **out);
+
+int sgw_graph_info(const sgw_graph *g, uint32_t *n, uint32_t *m, int *weighted);
+const uint32_t *sgw_graph_node_pointer(const sgw_graph *g);
+const void *sgw_graph_edges(const sgw_graph *g);
+/* outDegree[i] = nodePointer[i+1] - nodePointer[i] for all i
+ * (shared/graph.cu:177-181 with every entry written). */
+int sgw_graph_out_degree(const sgw_graph *g, uint32_t *out_degree);
+/* Writes .bcsr/.bwcsr (tools/converter.cpp:88-95, :157-164) or .el/.wel
+ * text, chosen by extension. */
+int sgw_graph_save(const sgw_graph *g, const char *path);
+void sgw_graph_free(sgw_graph *g);
+
+/* ---- engine --------------------------------------------------------------- */
+#define SGW_OPT_PROFILE   0x1u  /* time every kernel class with CUDA events   */
+#define SGW_OPT_NO_OVERLAP 0x2u /* one edge buffer, no copy/compute overlap   */
+
+typedef struct sgw_engine_opts {
+  /* Device-memory budget in bytes for everything the engine allocates.
+   * 0 = the reference's rule: 0.9 * (totalGlobalMem - 32 n) bytes of edges
+   * (shared/subgraph.cu:24-28) plus the vertex state. */
+  uint64_t budget_bytes;
+  int32_t device;          /* CUDA device ordinal (--device)                  */
+  uint32_t flags;          /* SGW_OPT_*                                       */
+  uint32_t inner_batch;    /* async inner iterations launched per host check  */
+  uint32_t tile_degree_max;/* sources above this degree go to the chunk list  */
+  uint32_t chunk_edges;    /* edges per chunk-list item (multiple of 32)      */
+  uint32_t reserved[8];
+} sgw_engine_opts;
+
+void sgw_engine_opts_default(sgw_engine_opts *opts);
+
+/* Creates the device vertex state and edge buffers under the budget and
+ * registers the graph's host edges for device access.  Replaces the
+ * allocation side of Graph<E>::ReadGraph (shared/graph.cu:187-190),
+ * Subgraph<E>::Subgraph (shared/subgraph.cu:9-42) and
+ * SubgraphGenerator<E>::SubgraphGenerator (shared/subgraph_generator.cu:100-126). */
+int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts,
+                      sgw_engine **out);
+int sgw_engine_destroy(sgw_engine *e);
+
+/* max_partition_size: edges one device edge buffer holds
+ * (Subgraph<E>::max_partition_size, shared/subgraph.cu:24-28). */
+int sgw_engine_max_partition_size(const sgw_engine *e, uint64_t *edges);
+/* Device bytes the engine holds (always <= the budget). */
+int sgw_engine_device_bytes(const sgw_engine *e, uint64_t *bytes);
+
+typedef struct sgw_run_params {
+  int32_t algo;            /* SGW_BFS .. SGW_PR                               */
+  int32_t mode;            /* SGW_SYNC / SGW_ASYNC                            */
+  uint32_t source;         /* --source (ignored by CC and PR)                 */
+  float pr_init;           /* initial delta, 0.15 (subway/pr-sync.cu:33)      */
+  float pr_acc;            /* activation threshold, 0.01 (subway/pr-sync.cu:34) */
+  float pr_damping;        /* 0.85 (shared/gpu_kernels.cu:239)                */
+  uint32_t max_inner;      /* async: inner iterations per partition visit,
+                              0 = until the partition converges (reference)  */
+  uint32_t reserved[7];
+} sgw_run_params;
+
+void sgw_run_params_default(sgw_run_params *p, int algo, int mode, uint32_t source);
+
+typedef struct sgw_run_stats {
+  uint32_t global_iterations;   /* "Number of iterations" (subway/bfs-sync.cu:94) */
+  uint32_t partitions;          /* partitions processed, summed over iterations */
+  uint64_t inner_iterations;    /* async inner iterations, summed               */
+  uint64_t active_vertices;     /* queued (degree > 0) vertices, summed         */
+  uint64_t active_edges;        /* edges of queued vertices, summed             */
+  uint64_t h2d_bytes;           /* bytes read from host memory by the device    */
+  uint64_t d2h_bytes;           /* bytes copied device -> host                  */
+  uint64_t reached_edges;       /* edges whose source has a final label that is
+                                   not the initial one (Graph500 m_reached)     */
+  double ms_device;             /* CUDA-event time of the processing loop       */
+  double ms_generate;           /* SGW_OPT_PROFILE: per kernel class totals     */
+  double ms_partition;
+  double ms_gather;
+  double ms_relax;
+  uint64_t launches;            /* kernels launched by the run                  */
+  uint64_t gather_launches;
+  uint64_t relax_launches;
+  uint64_t generate_launches;
+  uint64_t reserved[4];
+} sgw_run_stats;
+
+/* One whole application run: the init loops, the first generate, the
+ * global-iteration / partition / inner-iteration loops and the final value
+ * read-back of subway/<algo>-<mode>.cu (e.g. subway/sssp-async.cu:38-127).
+ * out_values: host buffer of n uint32 (float for PR).  stats may be NULL. */
+int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values,
+            sgw_run_stats *stats);
+
+/* ---- step API: the reference's role classes, one call per role ------- */
+
+/* The per-app initial state (values, label1/label2; PR delta/value), e.g.
+ * subway/sssp-async.cu:38-51 and :59-64, and the first generate
+ * (:57).  Leaves the engine ready for sgw_partition. */
+int sgw_state_init(sgw_engine *e, const sgw_run_params *p);
+/* SubgraphGenerator<E>::generate (shared/subgraph_generator.cu:128-204,
+ * :209-285): activeness, scan, compaction.  Returns the number of queued
+ * vertices and their edges. */
+int sgw_generate(sgw_engine *e, uint32_t *num_active_nodes,
+                 uint64_t *num_active_edges);
+/* Partitioner<E>::partition (shared/partitioner.cu:12-91). */
+int sgw_partition(sgw_engine *e, uint32_t *num_partitions);
+int sgw_partition_info(const sgw_engine *e, uint32_t i, uint32_t *from_node,
+                       uint32_t *from_edge, uint32_t *node_size,
+                       uint64_t *edge_size);
+/* One partition of one global iteration: the transfer, the label hand-off
+ * (moveUpLabels / mixLabels, shared/gpu_kernels.cu:515-534) and the
+ * relaxation kernel or async inner loop (subway/sssp-async.cu:85-117). */
+int sgw_process_partition(sgw_engine *e, uint32_t i, uint32_t *inner_iterations);
+/* Device -> host copy of the values (subway/sssp-async.cu:127). */
+int sgw_read_values(sgw_engine *e, void *out_values);
+/* PR only: the engine's double-precision values. */
+int sgw_read_values_f64(sgw_engine *e, double *out_values);
+/* The compacted active queue of the last generate: activeNodes and
+ * activeNodesPointer (shared/subgraph.cuh:19-20); ptr has count+1 entries. */
+int sgw_read_active(sgw_engine *e, uint32_t *nodes, uint32_t *ptr,
+                    uint32_t capacity, uint32_t *count);
+
+/* Statistics accumulated since the last sgw_state_init / sgw_run. */
+int sgw_get_stats(const sgw_engine *e, sgw_run_stats *stats);
+
+/* Partition planning on the host: the greedy split of a compacted active
+ * queue (prefix array ptr of count+1 entries) into runs whose edge count is
+ * at most cap; a vertex with more than cap edges gets a run of its own.
+ * Same routine the device planner runs.  Replaces the binary search of
+ * shared/partitioner.cu:29-91 (which never ends when one vertex exceeds the
+ * budget).  Returns the number of runs; from/size arrays get one entry each
+ * (capacity entries at most). */
+int sgw_plan_partitions(const uint32_t *ptr, uint32_t count, uint64_t cap,
+                        uint32_t *from_node, uint32_t *node_size,
+                        uint32_t capacity, uint32_t *num_partitions);
+
+/* Number of CUDA devices visible (0 on a machine without a GPU). */
+int sgw_device_count(int *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SUBWAY_GB300_H */

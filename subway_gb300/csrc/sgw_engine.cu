@@ -1,0 +1,834 @@
+// Device half of libsubwaygb: the engine object, its budgeted device arena,
+// the global-iteration / partition / inner-iteration loops and the C ABI.
+//
+// Reference control flow: subway/sssp-async.cu:53-127 (async) and
+// subway/bfs-sync.cu:44-98 (sync); roles shared/subgraph.cu,
+// shared/subgraph_generator.cu, shared/partitioner.cu.
+
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "sgw_internal.h"
+#include "sgw_kernels.cuh"
+
+using namespace sgw;
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t _e = (call);                                                      \
+    if (_e != cudaSuccess)                                                        \
+      return fail(SGW_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), \
+                  __FILE__, __LINE__);                                            \
+  } while (0)
+
+#define TRY(call)                \
+  do {                           \
+    int _s = (call);             \
+    if (_s != SGW_OK) return _s; \
+  } while (0)
+
+namespace {
+
+enum KClass { K_GENERATE = 0, K_PLAN, K_GATHER, K_RELAX, K_NCLASS };
+
+struct ProfEvent {
+  int cls;
+  cudaEvent_t a, b;
+};
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct sgw_engine {
+  const sgw_graph *g = nullptr;
+  int device = 0;
+  int num_sms = 0;
+  sgw_engine_opts opts{};
+  uint64_t budget = 0;
+  uint32_t n = 0, m = 0, W = 1;  // W: u32 words per edge record
+
+  // device arena
+  char *d_arena = nullptr;
+  size_t arena_bytes = 0;
+  uint32_t *d_off = nullptr;
+  uint32_t *d_value = nullptr;
+  uint8_t *d_l1 = nullptr, *d_l2 = nullptr;
+  uint32_t *d_queue = nullptr, *d_ptr = nullptr;
+  uint32_t *d_tflag = nullptr;
+  unsigned long long *d_tagg = nullptr, *d_tincl = nullptr;
+  Ctl *d_ctl = nullptr;
+  Part *d_parts = nullptr;
+  WorkItem *d_wl = nullptr;
+  uint32_t *d_buf[2] = {nullptr, nullptr};
+  uint64_t cap = 0;  // edges per buffer
+  uint32_t nbuf = 2;
+  uint32_t max_parts = 0, wl_cap = 0, num_tiles = 0;
+
+  // host side
+  Ctl *h_ctl = nullptr;
+  Part *h_parts = nullptr;
+  const uint32_t *d_host_edges = nullptr;
+  bool registered = false;
+  cudaStream_t s_comp = nullptr, s_copy = nullptr;
+  cudaEvent_t ev_ready[2] = {}, ev_free[2] = {};
+  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+  std::vector<ProfEvent> prof;
+  size_t prof_used = 0;
+  uint32_t epoch = 0;
+
+  // run state
+  sgw_run_params params{};
+  bool initialized = false;
+  uint32_t num_active = 0;
+  uint64_t num_active_edges = 0;
+  uint32_t num_parts = 0;
+  bool parts_valid = false;
+  sgw_run_stats stats{};
+};
+
+namespace {
+
+// ---- timing helpers -----------------------------------------------------------
+int prof_begin(sgw_engine *e, int cls, cudaStream_t s, size_t *slot) {
+  if (!(e->opts.flags & SGW_OPT_PROFILE)) return SGW_OK;
+  if (e->prof_used == e->prof.size()) {
+    ProfEvent pe;
+    pe.cls = cls;
+    CK(cudaEventCreate(&pe.a));
+    CK(cudaEventCreate(&pe.b));
+    e->prof.push_back(pe);
+  }
+  *slot = e->prof_used++;
+  e->prof[*slot].cls = cls;
+  CK(cudaEventRecord(e->prof[*slot].a, s));
+  return SGW_OK;
+}
+
+int prof_end(sgw_engine *e, cudaStream_t s, size_t slot) {
+  if (!(e->opts.flags & SGW_OPT_PROFILE)) return SGW_OK;
+  CK(cudaEventRecord(e->prof[slot].b, s));
+  return SGW_OK;
+}
+
+int prof_collect(sgw_engine *e) {
+  double ms[K_NCLASS] = {0, 0, 0, 0};
+  for (size_t i = 0; i < e->prof_used; ++i) {
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, e->prof[i].a, e->prof[i].b));
+    ms[e->prof[i].cls] += t;
+  }
+  e->prof_used = 0;
+  e->stats.ms_generate += ms[K_GENERATE];
+  e->stats.ms_partition += ms[K_PLAN];
+  e->stats.ms_gather += ms[K_GATHER];
+  e->stats.ms_relax += ms[K_RELAX];
+  return SGW_OK;
+}
+
+int check_ctl_error(sgw_engine *e) {
+  uint32_t err = e->h_ctl->error;
+  if (err == 0) return SGW_OK;
+  if (err == 1) return fail(SGW_ETIMEOUT, "scan look-back wait timed out");
+  if (err == 2) return fail(SGW_ERANGE, "partition table overflow");
+  if (err == 3) return fail(SGW_ERANGE, "chunk list overflow");
+  if (err == 4) return fail(SGW_ESTATE, "scan ticket counter out of step");
+  return fail(SGW_ECUDA, "device error code %u", err);
+}
+
+int read_ctl(sgw_engine *e) {
+  CK(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
+  e->stats.d2h_bytes += sizeof(Ctl);
+  CK(cudaStreamSynchronize(e->s_comp));
+  return check_ctl_error(e);
+}
+
+// ---- arena layout ------------------------------------------------------------------
+struct Layout {
+  size_t off, value, l1, l2, queue, ptr, tflag, tagg, tincl, ctl, parts, wl, buf0, buf1, total;
+  uint64_t cap;
+  uint32_t max_parts, wl_cap;
+};
+
+size_t fixed_bytes(uint32_t n, uint32_t num_tiles) {
+  size_t b = 0;
+  b += align_up(4ull * (n + 1), 256);   // off
+  b += align_up(4ull * n, 256);         // value
+  b += 2 * align_up(n, 256);            // l1, l2
+  b += align_up(4ull * n, 256);         // queue
+  b += align_up(4ull * (n + 1), 256);   // ptr
+  b += align_up(4ull * num_tiles, 256) + 2 * align_up(8ull * num_tiles, 256);
+  b += align_up(sizeof(Ctl), 256);
+  return b;
+}
+
+Layout make_layout(uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf, uint32_t num_tiles,
+                   uint64_t cap, uint32_t chunk, uint32_t tdm) {
+  Layout L{};
+  size_t p = 0;
+  auto take = [&](size_t bytes) { size_t at = p; p += align_up(bytes, 256); return at; };
+  L.off = take(4ull * (n + 1));
+  L.value = take(4ull * n);
+  L.l1 = take(n);
+  L.l2 = take(n);
+  L.queue = take(4ull * n);
+  L.ptr = take(4ull * (n + 1));
+  L.tflag = take(4ull * num_tiles);
+  L.tagg = take(8ull * num_tiles);
+  L.tincl = take(8ull * num_tiles);
+  L.ctl = take(sizeof(Ctl));
+  L.cap = cap;
+  L.max_parts = (uint32_t)std::min<uint64_t>(2ull * ((uint64_t)m / cap + 1) + 2, 0x7fffffffull);
+  L.wl_cap = (uint32_t)std::min<uint64_t>(cap / chunk + cap / std::max<uint32_t>(tdm, 1) + 64, 0x7fffffffull);
+  L.parts = take(sizeof(Part) * (size_t)L.max_parts);
+  L.wl = take(sizeof(WorkItem) * (size_t)L.wl_cap);
+  L.buf0 = take(cap * esz);
+  L.buf1 = nbuf > 1 ? take(cap * esz) : L.buf0;
+  L.total = p;
+  return L;
+}
+
+int carve(sgw_engine *e, const Layout &L) {
+  char *b = e->d_arena;
+  e->d_off = (uint32_t *)(b + L.off);
+  e->d_value = (uint32_t *)(b + L.value);
+  e->d_l1 = (uint8_t *)(b + L.l1);
+  e->d_l2 = (uint8_t *)(b + L.l2);
+  e->d_queue = (uint32_t *)(b + L.queue);
+  e->d_ptr = (uint32_t *)(b + L.ptr);
+  e->d_tflag = (uint32_t *)(b + L.tflag);
+  e->d_tagg = (unsigned long long *)(b + L.tagg);
+  e->d_tincl = (unsigned long long *)(b + L.tincl);
+  e->d_ctl = (Ctl *)(b + L.ctl);
+  e->d_parts = (Part *)(b + L.parts);
+  e->d_wl = (WorkItem *)(b + L.wl);
+  e->d_buf[0] = (uint32_t *)(b + L.buf0);
+  e->d_buf[1] = (uint32_t *)(b + L.buf1);
+  e->cap = L.cap;
+  e->max_parts = L.max_parts;
+  e->wl_cap = L.wl_cap;
+  return SGW_OK;
+}
+
+// ---- launch helpers ---------------------------------------------------------------
+uint32_t grid_for(const sgw_engine *e, uint64_t items, uint32_t per_cta) {
+  uint64_t g = (items + per_cta - 1) / per_cta;
+  uint64_t mx = (uint64_t)e->num_sms * 8;
+  return (uint32_t)std::max<uint64_t>(1, std::min(g, mx));
+}
+
+int launch_generate(sgw_engine *e, int consume) {
+  GenArgs a;
+  a.n = e->n;
+  a.l1 = e->d_l1;
+  a.l2 = e->d_l2;
+  a.off = e->d_off;
+  a.queue = e->d_queue;
+  a.ptr = e->d_ptr;
+  a.tflag = e->d_tflag;
+  a.tagg = e->d_tagg;
+  a.tincl = e->d_tincl;
+  a.ctl = e->d_ctl;
+  e->epoch = (e->epoch + 1) & 0x3fffffffu;
+  if (e->epoch == 0) e->epoch = 1;
+  a.epoch = e->epoch;
+  a.num_tiles = e->num_tiles;
+  a.consume = consume;
+  CK(cudaMemsetAsync(&e->d_ctl->num_seen, 0, sizeof(uint32_t), e->s_comp));
+  size_t slot = 0;
+  TRY(prof_begin(e, K_GENERATE, e->s_comp, &slot));
+  k_generate<<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  CK(cudaGetLastError());
+  TRY(prof_end(e, e->s_comp, slot));
+  e->stats.launches += 1;
+  e->stats.generate_launches += 1;
+  e->parts_valid = false;
+  return SGW_OK;
+}
+
+int launch_plan(sgw_engine *e) {
+  size_t slot = 0;
+  TRY(prof_begin(e, K_PLAN, e->s_comp, &slot));
+  k_plan<<<1, 32, 0, e->s_comp>>>(e->d_ptr, e->d_queue, e->d_ctl, e->d_parts, e->max_parts,
+                                   (unsigned long long)e->cap);
+  CK(cudaGetLastError());
+  TRY(prof_end(e, e->s_comp, slot));
+  e->stats.launches += 1;
+  return SGW_OK;
+}
+
+// generate + plan + one read-back: the per-global-iteration host sync.
+int generate_and_plan(sgw_engine *e, int consume) {
+  TRY(launch_generate(e, consume));
+  TRY(launch_plan(e));
+  CK(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
+  CK(cudaStreamSynchronize(e->s_comp));
+  TRY(check_ctl_error(e));
+  e->num_active = e->h_ctl->num_active;
+  e->num_active_edges = e->h_ctl->num_active_edges;
+  e->num_parts = e->h_ctl->num_parts;
+  if (e->num_parts > 0) {
+    CK(cudaMemcpyAsync(e->h_parts, e->d_parts, sizeof(Part) * e->num_parts,
+                       cudaMemcpyDeviceToHost, e->s_comp));
+    CK(cudaStreamSynchronize(e->s_comp));
+  }
+  e->stats.d2h_bytes += sizeof(Ctl) + sizeof(Part) * e->num_parts;
+  e->parts_valid = true;
+  return SGW_OK;
+}
+
+bool is_hub(const sgw_engine *e, const Part &p) { return p.edge_count > e->cap; }
+
+int enqueue_gather(sgw_engine *e, uint32_t p, cudaStream_t s) {
+  const Part &q = e->h_parts[p];
+  const uint32_t b = p % e->nbuf;
+  if (is_hub(e, q) || q.edge_count == 0) return SGW_OK;
+  CK(cudaStreamWaitEvent(s, e->ev_free[b], 0));
+  size_t slot = 0;
+  TRY(prof_begin(e, K_GATHER, s, &slot));
+  const uint32_t grid = grid_for(e, q.edge_count, kGatherTile);
+  if (e->W == 1)
+    k_gather<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_edges,
+                                                e->d_buf[b], q.from, q.size, q.edge_from,
+                                                (uint32_t)q.edge_count);
+  else
+    k_gather<2><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_edges,
+                                                e->d_buf[b], q.from, q.size, q.edge_from,
+                                                (uint32_t)q.edge_count);
+  CK(cudaGetLastError());
+  TRY(prof_end(e, s, slot));
+  CK(cudaEventRecord(e->ev_ready[b], s));
+  e->stats.h2d_bytes += q.edge_count * 4ull * e->W;
+  e->stats.launches += 1;
+  e->stats.gather_launches += 1;
+  return SGW_OK;
+}
+
+template <int ALGO, bool ASYNC, int W>
+int launch_relax_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, uint8_t *cur,
+                      uint8_t *nxt) {
+  RelaxArgs a;
+  a.queue = e->d_queue;
+  a.ptr = e->d_ptr;
+  a.buf = e->d_buf[b];
+  a.value = e->d_value;
+  a.cur = cur;
+  a.nxt = nxt;
+  a.ctl = e->d_ctl;
+  a.wl = e->d_wl;
+  a.wl_cap = e->wl_cap;
+  a.from = q.from;
+  a.size = q.size;
+  a.edge_from = q.edge_from;
+  a.iter = iter;
+  a.tile_degree_max = e->opts.tile_degree_max;
+  a.chunk_edges = e->opts.chunk_edges;
+  const uint32_t g1 = grid_for(e, q.size, kRelaxThreads);
+  k_relax_tile<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
+  CK(cudaGetLastError());
+  k_relax_chunks<ALGO, ASYNC, W><<<e->num_sms * 4, kRelaxThreads, 0, e->s_comp>>>(a);
+  CK(cudaGetLastError());
+  e->stats.launches += 2;
+  e->stats.relax_launches += 2;
+  return SGW_OK;
+}
+
+template <int ALGO, int W>
+int relax_dispatch_w(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, bool async,
+                     uint8_t *cur, uint8_t *nxt) {
+  if (async) return launch_relax_pair<ALGO, true, W>(e, q, b, iter, cur, nxt);
+  return launch_relax_pair<ALGO, false, W>(e, q, b, iter, cur, nxt);
+}
+
+template <int ALGO>
+int relax_dispatch(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, bool async,
+                   uint8_t *cur, uint8_t *nxt) {
+  if (e->W == 1) return relax_dispatch_w<ALGO, 1>(e, q, b, iter, async, cur, nxt);
+  return relax_dispatch_w<ALGO, 2>(e, q, b, iter, async, cur, nxt);
+}
+
+int launch_relax(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, bool async) {
+  uint8_t *cur = e->d_l1, *nxt = e->d_l2;
+  if (async && (iter % 2 == 0)) std::swap(cur, nxt);  // ping-pong (sssp-async.cu:108-109)
+  switch (e->params.algo) {
+    case SGW_BFS: return relax_dispatch<SGW_BFS>(e, q, b, iter, async, cur, nxt);
+    case SGW_SSSP: return relax_dispatch<SGW_SSSP>(e, q, b, iter, async, cur, nxt);
+    case SGW_SSWP: return relax_dispatch<SGW_SSWP>(e, q, b, iter, async, cur, nxt);
+    case SGW_CC: return relax_dispatch<SGW_CC>(e, q, b, iter, async, cur, nxt);
+    default: return fail(SGW_EINVAL, "algorithm %d not supported", e->params.algo);
+  }
+}
+
+template <int ALGO, int W>
+int launch_flat_w(sgw_engine *e, uint32_t b, uint32_t count) {
+  k_relax_flat<ALGO, W><<<grid_for(e, count, 256), 256, 0, e->s_comp>>>(e->d_buf[b], count, e->d_value,
+                                                                       e->d_l2, e->d_ctl);
+  CK(cudaGetLastError());
+  return SGW_OK;
+}
+template <int ALGO>
+int launch_flat(sgw_engine *e, uint32_t b, uint32_t count) {
+  return e->W == 1 ? launch_flat_w<ALGO, 1>(e, b, count) : launch_flat_w<ALGO, 2>(e, b, count);
+}
+
+// A single vertex whose edges exceed one buffer: claim it once, then stream
+// and relax its edges piece by piece (one inner iteration).
+int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
+  const bool async = e->params.mode == SGW_ASYNC;
+  const uint32_t u = q.first_vertex;
+  if (async) k_hub_claim<true><<<1, 1, 0, e->s_comp>>>(u, e->d_value, e->d_l1, e->d_l2, e->d_ctl);
+  else k_hub_claim<false><<<1, 1, 0, e->s_comp>>>(u, e->d_value, e->d_l1, e->d_l2, e->d_ctl);
+  CK(cudaGetLastError());
+  const uint64_t deg = q.edge_count;
+  const uint64_t hoff = e->g->node_pointer[u];
+  const size_t esz = 4ull * e->W;
+  for (uint64_t s = 0; s < deg; s += e->cap) {
+    const uint32_t cnt = (uint32_t)std::min<uint64_t>(e->cap, deg - s);
+    size_t slot = 0;
+    TRY(prof_begin(e, K_GATHER, e->s_comp, &slot));
+    CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->g->edges + (hoff + s) * esz, cnt * esz,
+                       cudaMemcpyHostToDevice, e->s_comp));
+    TRY(prof_end(e, e->s_comp, slot));
+    e->stats.h2d_bytes += cnt * esz;
+    TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
+    int st;
+    switch (e->params.algo) {
+      case SGW_BFS: st = launch_flat<SGW_BFS>(e, b, cnt); break;
+      case SGW_SSSP: st = launch_flat<SGW_SSSP>(e, b, cnt); break;
+      case SGW_SSWP: st = launch_flat<SGW_SSWP>(e, b, cnt); break;
+      default: st = launch_flat<SGW_CC>(e, b, cnt); break;
+    }
+    TRY(st);
+    TRY(prof_end(e, e->s_comp, slot));
+    e->stats.launches += 1;
+    e->stats.relax_launches += 1;
+  }
+  e->stats.inner_iterations += 1;
+  return SGW_OK;
+}
+
+// Relaxation of one resident partition: sync = one pass; async = mixLabels
+// then inner iterations until no relaxation improves (or max_inner).
+int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_out) {
+  const bool async = e->params.mode == SGW_ASYNC;
+  CK(cudaMemsetAsync(&e->d_ctl->upd[0], 0, sizeof(uint32_t) * 9, e->s_comp));  // upd, wl_count, iters_run
+  if (!async) {
+    size_t slot = 0;
+    TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
+    TRY(launch_relax(e, q, b, 1, false));
+    TRY(prof_end(e, e->s_comp, slot));
+    e->stats.inner_iterations += 1;
+    if (iters_out) *iters_out = 1;
+    return SGW_OK;
+  }
+  k_mix<<<grid_for(e, q.size, 256), 256, 0, e->s_comp>>>(e->d_queue, q.from, q.size, e->d_l1, e->d_l2);
+  CK(cudaGetLastError());
+  e->stats.launches += 1;
+  const uint32_t max_inner = e->params.max_inner ? e->params.max_inner : 0xffffffffu;
+  uint32_t iter = 1;
+  const uint32_t batch = std::max<uint32_t>(1, e->opts.inner_batch);
+  while (true) {
+    const uint32_t nb = std::min<uint32_t>(batch, max_inner - (iter - 1));
+    size_t slot = 0;
+    TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
+    for (uint32_t k = 0; k < nb; ++k, ++iter) TRY(launch_relax(e, q, b, iter, true));
+    TRY(prof_end(e, e->s_comp, slot));
+    TRY(read_ctl(e));
+    const uint32_t last = iter - 1;
+    if (e->h_ctl->upd[last & 3u] == 0) break;  // converged
+    if (last >= max_inner) break;             // leftover labels go to the next generate
+  }
+  const uint32_t ran = e->h_ctl->iters_run;
+  e->stats.inner_iterations += ran;
+  if (iters_out) *iters_out = ran;
+  return SGW_OK;
+}
+
+int validate_params(const sgw_engine *e, const sgw_run_params *p) {
+  if (!p) return fail(SGW_EINVAL, "null params");
+  if (p->algo < SGW_BFS || p->algo > SGW_PR) return fail(SGW_EINVAL, "bad algorithm %d", p->algo);
+  if (p->mode != SGW_SYNC && p->mode != SGW_ASYNC) return fail(SGW_EINVAL, "bad mode %d", p->mode);
+  if (p->algo == SGW_PR) return fail(SGW_EINVAL, "PageRank is not available in this build");
+  if ((p->algo == SGW_SSSP || p->algo == SGW_SSWP) && !e->g->weighted)
+    return fail(SGW_EINVAL, "SSSP/SSWP need a weighted graph (.bwcsr/.wel)");
+  if (p->algo != SGW_CC && p->source >= e->n)
+    return fail(SGW_EINVAL, "source %u out of range (n=%u)", p->source, e->n);
+  return SGW_OK;
+}
+
+int state_init(sgw_engine *e, const sgw_run_params *p) {
+  TRY(validate_params(e, p));
+  CK(cudaSetDevice(e->device));
+  e->params = *p;
+  e->stats = sgw_run_stats{};
+  e->prof_used = 0;
+  e->initialized = false;
+  const uint32_t src = p->algo == SGW_CC ? 0xffffffffu : p->source;
+  k_init<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->algo, p->mode, src, e->d_value,
+                                                        e->d_l1, e->d_l2);
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(e->d_ctl, 0, sizeof(Ctl), e->s_comp));
+  e->stats.launches += 1;
+  const bool async = p->mode == SGW_ASYNC;
+  TRY(generate_and_plan(e, async ? 0 : 1));
+  if (async && p->algo != SGW_CC) {
+    k_async_reset<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->source, e->d_l1);
+    CK(cudaGetLastError());
+    e->stats.launches += 1;
+  }
+  e->initialized = true;
+  return SGW_OK;
+}
+
+// All partitions of one global iteration, gathers double-buffered on the
+// copy stream against relaxation on the compute stream.
+int process_iteration(sgw_engine *e) {
+  const uint32_t P = e->num_parts;
+  if (P == 0) return SGW_OK;
+  TRY(enqueue_gather(e, 0, e->s_copy));
+  for (uint32_t p = 0; p < P; ++p) {
+    const Part &q = e->h_parts[p];
+    const uint32_t b = p % e->nbuf;
+    if (e->nbuf > 1 && p + 1 < P) TRY(enqueue_gather(e, p + 1, e->s_copy));
+    if (is_hub(e, q)) {
+      TRY(process_hub(e, q, b));
+    } else {
+      CK(cudaStreamWaitEvent(e->s_comp, e->ev_ready[b], 0));
+      TRY(process_resident(e, q, b, nullptr));
+    }
+    CK(cudaEventRecord(e->ev_free[b], e->s_comp));
+    if (e->nbuf == 1 && p + 1 < P) TRY(enqueue_gather(e, p + 1, e->s_copy));
+    e->stats.partitions += 1;
+  }
+  return SGW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sgw_engine_opts_default(sgw_engine_opts *o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->budget_bytes = 0;
+  o->device = 0;
+  o->flags = 0;
+  o->inner_batch = 8;
+  o->tile_degree_max = 256;
+  o->chunk_edges = 1024;
+}
+
+void sgw_run_params_default(sgw_run_params *p, int algo, int mode, uint32_t source) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->algo = algo;
+  p->mode = mode;
+  p->source = source;
+  p->pr_init = 0.15f;
+  p->pr_acc = 0.01f;
+  p->pr_damping = 0.85f;
+  p->max_inner = 0;
+}
+
+int sgw_device_count(int *count) {
+  if (!count) return fail(SGW_EINVAL, "null argument");
+  int c = 0;
+  if (cudaGetDeviceCount(&c) != cudaSuccess) c = 0;
+  cudaGetLastError();
+  *count = c;
+  return SGW_OK;
+}
+
+int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_engine **out) {
+  clear_error();
+  if (!g || !out) return fail(SGW_EINVAL, "null argument");
+  *out = nullptr;
+  sgw_engine_opts o;
+  sgw_engine_opts_default(&o);
+  if (opts_in) o = *opts_in;
+  if (o.inner_batch == 0) o.inner_batch = 8;
+  if (o.tile_degree_max == 0) o.tile_degree_max = 256;
+  if (o.chunk_edges == 0) o.chunk_edges = 1024;
+  if (o.chunk_edges % 32) return fail(SGW_EINVAL, "chunk_edges must be a multiple of 32");
+  if (g->weighted && (((uintptr_t)g->edges) & 7u)) return fail(SGW_EINVAL, "edges must be 8-byte aligned");
+  if (g->n >= 0x80000000u) return fail(SGW_ERANGE, "vertex count %u above 2^31", g->n);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(SGW_ECUDA, "no CUDA device");
+  }
+  if (o.device < 0 || o.device >= ndev) return fail(SGW_EINVAL, "device %d out of range", o.device);
+  CK(cudaSetDevice(o.device));
+
+  sgw_engine *e = new (std::nothrow) sgw_engine();
+  if (!e) return fail(SGW_ENOMEM, "engine object");
+  e->g = g;
+  e->device = o.device;
+  e->opts = o;
+  e->n = g->n;
+  e->m = g->m;
+  e->W = g->weighted ? 2 : 1;
+  e->nbuf = (o.flags & SGW_OPT_NO_OVERLAP) ? 1 : 2;
+  e->num_tiles = (uint32_t)((g->n + kGenTile - 1) / kGenTile);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, o.device) != cudaSuccess) { delete e; return fail(SGW_ECUDA, "device properties"); }
+  e->num_sms = prop.multiProcessorCount;
+
+  const uint32_t esz = 4 * e->W;
+  const size_t F = fixed_bytes(e->n, e->num_tiles);
+  const double per_edge = (double)e->nbuf * esz + 16.0 / o.chunk_edges + 16.0 / o.tile_degree_max;
+  uint64_t budget = o.budget_bytes;
+  if (budget == 0) {
+    // Subway's rule: 0.9 * (totalGlobalMem - 32 n) bytes of edges
+    // (shared/subgraph.cu:24), here on top of the engine's own vertex state.
+    double edges_bytes = 0.9 * ((double)prop.totalGlobalMem - 32.0 * e->n);
+    budget = (uint64_t)(F + std::max(0.0, edges_bytes)) ;
+  }
+  uint64_t cap_full = std::max<uint64_t>(e->m, 1);
+  const size_t slack = 64 * 1024 + 8 * 256;
+  if (budget < F + slack + 64 * per_edge) {
+    delete e;
+    return fail(SGW_EBUDGET, "budget %llu B < vertex state %zu B + minimum edge buffers",
+                (unsigned long long)budget, F);
+  }
+  uint64_t cap = (uint64_t)((double)(budget - F - slack) / per_edge);
+  cap = std::min<uint64_t>(cap, cap_full);
+  cap = std::min<uint64_t>(cap, 4294967294ull);  // max_partition_size <= DIST_INFINITY
+  Layout L = make_layout(e->n, e->m, esz, e->nbuf, e->num_tiles, cap, o.chunk_edges, o.tile_degree_max);
+  while (L.total > budget && cap > 64) {
+    cap = cap - std::max<uint64_t>(cap / 64, 64);
+    L = make_layout(e->n, e->m, esz, e->nbuf, e->num_tiles, cap, o.chunk_edges, o.tile_degree_max);
+  }
+  if (L.total > budget) {
+    delete e;
+    return fail(SGW_EBUDGET, "budget %llu B too small (needs %zu B)", (unsigned long long)budget, L.total);
+  }
+  e->budget = budget;
+  cudaError_t ce = cudaMalloc(&e->d_arena, L.total);
+  if (ce != cudaSuccess) {
+    delete e;
+    return fail(SGW_ECUDA, "cudaMalloc(%zu): %s", L.total, cudaGetErrorString(ce));
+  }
+  e->arena_bytes = L.total;
+  carve(e, L);
+
+  int st = SGW_OK;
+  auto cleanup = [&](int s) { sgw_engine_destroy(e); return s; };
+  // host edges readable by device kernels (mapped pinned memory)
+  const size_t ebytes = std::max<size_t>((size_t)e->m * esz, 4);
+  if (g->m > 0) {
+    size_t reg_bytes = g->owns ? g->edges_bytes_alloc : ebytes;
+    ce = cudaHostRegister(g->edges, reg_bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
+    if (ce == cudaSuccess) e->registered = true;
+    else if (ce == cudaErrorHostMemoryAlreadyRegistered) cudaGetLastError();
+    else { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostRegister: %s", cudaGetErrorString(ce))); }
+    void *dp = nullptr;
+    ce = cudaHostGetDevicePointer(&dp, g->edges, 0);
+    if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce))); }
+    e->d_host_edges = (const uint32_t *)dp;
+  }
+  if (cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(fail(SGW_ECUDA, "stream creation"));
+  for (int i = 0; i < 2; ++i) {
+    if (cudaEventCreateWithFlags(&e->ev_ready[i], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->ev_free[i], cudaEventDisableTiming) != cudaSuccess)
+      return cleanup(fail(SGW_ECUDA, "event creation"));
+  }
+  if (cudaEventCreate(&e->ev_t0) != cudaSuccess || cudaEventCreate(&e->ev_t1) != cudaSuccess)
+    return cleanup(fail(SGW_ECUDA, "event creation"));
+  if (cudaMallocHost(&e->h_ctl, sizeof(Ctl)) != cudaSuccess ||
+      cudaMallocHost(&e->h_parts, sizeof(Part) * (size_t)e->max_parts) != cudaSuccess)
+    return cleanup(fail(SGW_ECUDA, "pinned control block"));
+  memset(e->h_ctl, 0, sizeof(Ctl));
+  ce = cudaMemcpyAsync(e->d_off, g->node_pointer, 4ull * (e->n + 1), cudaMemcpyHostToDevice, e->s_comp);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_ctl, 0, sizeof(Ctl), e->s_comp);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_tflag, 0, 4ull * e->num_tiles, e->s_comp);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->s_comp);
+  if (ce != cudaSuccess) return cleanup(fail(SGW_ECUDA, "engine setup copies: %s", cudaGetErrorString(ce)));
+  (void)st;
+  *out = e;
+  return SGW_OK;
+}
+
+int sgw_engine_destroy(sgw_engine *e) {
+  if (!e) return SGW_OK;
+  cudaSetDevice(e->device);
+  if (e->s_comp) cudaStreamSynchronize(e->s_comp);
+  if (e->s_copy) cudaStreamSynchronize(e->s_copy);
+  for (auto &pe : e->prof) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
+  for (int i = 0; i < 2; ++i) {
+    if (e->ev_ready[i]) cudaEventDestroy(e->ev_ready[i]);
+    if (e->ev_free[i]) cudaEventDestroy(e->ev_free[i]);
+  }
+  if (e->ev_t0) cudaEventDestroy(e->ev_t0);
+  if (e->ev_t1) cudaEventDestroy(e->ev_t1);
+  if (e->s_comp) cudaStreamDestroy(e->s_comp);
+  if (e->s_copy) cudaStreamDestroy(e->s_copy);
+  if (e->h_ctl) cudaFreeHost(e->h_ctl);
+  if (e->h_parts) cudaFreeHost(e->h_parts);
+  if (e->registered) cudaHostUnregister(e->g->edges);
+  if (e->d_arena) cudaFree(e->d_arena);
+  cudaGetLastError();
+  delete e;
+  return SGW_OK;
+}
+
+int sgw_engine_max_partition_size(const sgw_engine *e, uint64_t *edges) {
+  if (!e || !edges) return fail(SGW_EINVAL, "null argument");
+  *edges = e->cap;
+  return SGW_OK;
+}
+
+int sgw_engine_device_bytes(const sgw_engine *e, uint64_t *bytes) {
+  if (!e || !bytes) return fail(SGW_EINVAL, "null argument");
+  *bytes = e->arena_bytes;
+  return SGW_OK;
+}
+
+int sgw_state_init(sgw_engine *e, const sgw_run_params *p) {
+  clear_error();
+  if (!e) return fail(SGW_EINVAL, "null engine");
+  return state_init(e, p);
+}
+
+int sgw_generate(sgw_engine *e, uint32_t *num_active_nodes, uint64_t *num_active_edges) {
+  clear_error();
+  if (!e || !e->initialized) return fail(SGW_ESTATE, "engine not initialised");
+  CK(cudaSetDevice(e->device));
+  TRY(launch_generate(e, e->params.mode == SGW_SYNC ? 1 : 0));
+  TRY(read_ctl(e));
+  e->num_active = e->h_ctl->num_active;
+  e->num_active_edges = e->h_ctl->num_active_edges;
+  if (num_active_nodes) *num_active_nodes = e->num_active;
+  if (num_active_edges) *num_active_edges = e->num_active_edges;
+  return SGW_OK;
+}
+
+int sgw_partition(sgw_engine *e, uint32_t *num_partitions) {
+  clear_error();
+  if (!e || !e->initialized) return fail(SGW_ESTATE, "engine not initialised");
+  CK(cudaSetDevice(e->device));
+  TRY(launch_plan(e));
+  TRY(read_ctl(e));
+  e->num_parts = e->h_ctl->num_parts;
+  if (e->num_parts) {
+    CK(cudaMemcpyAsync(e->h_parts, e->d_parts, sizeof(Part) * e->num_parts, cudaMemcpyDeviceToHost, e->s_comp));
+    CK(cudaStreamSynchronize(e->s_comp));
+  }
+  e->parts_valid = true;
+  if (num_partitions) *num_partitions = e->num_parts;
+  return SGW_OK;
+}
+
+int sgw_partition_info(const sgw_engine *e, uint32_t i, uint32_t *from_node, uint32_t *from_edge,
+                       uint32_t *node_size, uint64_t *edge_size) {
+  if (!e || !e->parts_valid) return fail(SGW_ESTATE, "no partition table");
+  if (i >= e->num_parts) return fail(SGW_EINVAL, "partition %u out of range", i);
+  const Part &q = e->h_parts[i];
+  if (from_node) *from_node = q.from;
+  if (from_edge) *from_edge = q.edge_from;
+  if (node_size) *node_size = q.size;
+  if (edge_size) *edge_size = q.edge_count;
+  return SGW_OK;
+}
+
+int sgw_process_partition(sgw_engine *e, uint32_t i, uint32_t *inner_iterations) {
+  clear_error();
+  if (!e || !e->initialized || !e->parts_valid) return fail(SGW_ESTATE, "no partition table");
+  if (i >= e->num_parts) return fail(SGW_EINVAL, "partition %u out of range", i);
+  CK(cudaSetDevice(e->device));
+  const Part &q = e->h_parts[i];
+  uint32_t iters = 1;
+  if (is_hub(e, q)) {
+    TRY(process_hub(e, q, 0));
+  } else {
+    TRY(enqueue_gather(e, i, e->s_comp));
+    TRY(process_resident(e, q, i % e->nbuf, &iters));
+  }
+  CK(cudaStreamSynchronize(e->s_comp));
+  TRY(read_ctl(e));
+  e->stats.partitions += 1;
+  if (inner_iterations) *inner_iterations = iters;
+  return SGW_OK;
+}
+
+int sgw_read_values(sgw_engine *e, void *out_values) {
+  clear_error();
+  if (!e || !out_values) return fail(SGW_EINVAL, "null argument");
+  if (!e->initialized) return fail(SGW_ESTATE, "engine not initialised");
+  CK(cudaSetDevice(e->device));
+  CK(cudaMemcpyAsync(out_values, e->d_value, 4ull * e->n, cudaMemcpyDeviceToHost, e->s_comp));
+  CK(cudaStreamSynchronize(e->s_comp));
+  e->stats.d2h_bytes += 4ull * e->n;
+  return SGW_OK;
+}
+
+int sgw_read_values_f64(sgw_engine *e, double *out_values) {
+  (void)e;
+  (void)out_values;
+  return fail(SGW_EINVAL, "PageRank is not available in this build");
+}
+
+int sgw_read_active(sgw_engine *e, uint32_t *nodes, uint32_t *ptr, uint32_t capacity, uint32_t *count) {
+  clear_error();
+  if (!e || !count) return fail(SGW_EINVAL, "null argument");
+  if (!e->initialized) return fail(SGW_ESTATE, "engine not initialised");
+  *count = e->num_active;
+  if (e->num_active > capacity) return fail(SGW_ERANGE, "capacity %u < %u", capacity, e->num_active);
+  CK(cudaSetDevice(e->device));
+  if (nodes && e->num_active)
+    CK(cudaMemcpyAsync(nodes, e->d_queue, 4ull * e->num_active, cudaMemcpyDeviceToHost, e->s_comp));
+  if (ptr)
+    CK(cudaMemcpyAsync(ptr, e->d_ptr, 4ull * (e->num_active + 1), cudaMemcpyDeviceToHost, e->s_comp));
+  CK(cudaStreamSynchronize(e->s_comp));
+  return SGW_OK;
+}
+
+int sgw_get_stats(const sgw_engine *e, sgw_run_stats *stats) {
+  if (!e || !stats) return fail(SGW_EINVAL, "null argument");
+  *stats = e->stats;
+  return SGW_OK;
+}
+
+int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values, sgw_run_stats *stats) {
+  clear_error();
+  if (!e) return fail(SGW_EINVAL, "null engine");
+  TRY(state_init(e, p));
+  const bool async = p->mode == SGW_ASYNC;
+  CK(cudaEventRecord(e->ev_t0, e->s_comp));  // "timer.Start()" after the first generate
+  uint32_t gitr = 0;
+  while (e->num_active > 0) {
+    ++gitr;
+    e->stats.active_vertices += e->num_active;
+    e->stats.active_edges += e->num_active_edges;
+    TRY(process_iteration(e));
+    TRY(generate_and_plan(e, async ? 0 : 1));
+  }
+  CK(cudaEventRecord(e->ev_t1, e->s_comp));
+  e->stats.global_iterations = gitr;
+  // Graph500 m_reached
+  const uint32_t src = p->algo == SGW_CC ? 0xffffffffu : p->source;
+  k_reached<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->algo, src, e->d_value, e->d_off, e->d_ctl);
+  CK(cudaGetLastError());
+  if (out_values) {
+    CK(cudaMemcpyAsync(out_values, e->d_value, 4ull * e->n, cudaMemcpyDeviceToHost, e->s_comp));
+    e->stats.d2h_bytes += 4ull * e->n;
+  }
+  CK(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
+  CK(cudaStreamSynchronize(e->s_comp));
+  TRY(check_ctl_error(e));
+  e->stats.reached_edges = e->h_ctl->reached_edges;
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e->ev_t0, e->ev_t1));
+  e->stats.ms_device = ms;
+  TRY(prof_collect(e));
+  if (stats) *stats = e->stats;
+  return SGW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,655 @@
+// Host half of libsubwaygb: graph objects, file formats, seeded generators,
+// connected-component helpers and the host partition planner.
+//
+// File formats follow the reference: binary CSR [u32 n][u32 m][u32
+// nodePointer x n][edge x m] (shared/graph.cu:39-52, tools/converter.cpp:
+// 88-95) and "src dst [w]" text lines (shared/graph.cu:56-170, README.md:16-30).
+
+#include <omp.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "sgw_graphgen.h"
+#include "sgw_internal.h"
+
+namespace sgw {
+
+static thread_local char g_err[512] = "";
+
+int fail(int status, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+void clear_error() { g_err[0] = 0; }
+
+static const size_t kPage = size_t(1) << 16;
+
+void *host_alloc(size_t bytes, size_t *rounded) {
+  size_t r = (bytes + kPage - 1) / kPage * kPage;
+  if (r == 0) r = kPage;
+  void *p = nullptr;
+  if (posix_memalign(&p, kPage, r) != 0) return nullptr;
+  if (rounded) *rounded = r;
+  return p;
+}
+
+void host_free(void *p) { free(p); }
+
+int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out) {
+  if (m >= (uint64_t(1) << 32))
+    return fail(SGW_ERANGE, "edge count %llu does not fit the u32 format",
+                (unsigned long long)m);
+  sgw_graph *g = new (std::nothrow) sgw_graph();
+  if (!g) return fail(SGW_ENOMEM, "graph object");
+  g->n = n;
+  g->m = (uint32_t)m;
+  g->weighted = weighted ? 1 : 0;
+  g->esz = weighted ? 8 : 4;
+  g->owns = true;
+  g->node_pointer = (uint32_t *)host_alloc(sizeof(uint32_t) * (size_t(n) + 1), nullptr);
+  g->edges = host_alloc(size_t(m) * g->esz, &g->edges_bytes_alloc);
+  if (!g->node_pointer || !g->edges) {
+    host_free(g->node_pointer);
+    host_free(g->edges);
+    delete g;
+    return fail(SGW_ENOMEM, "graph arrays (n=%u m=%llu)", n, (unsigned long long)m);
+  }
+  *out = g;
+  return SGW_OK;
+}
+
+// ---- SplitMix64 ------------------------------------------------------------
+static inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+static const uint64_t kGamma = 0x9e3779b97f4a7c15ULL;
+
+struct SplitMix {
+  uint64_t s;
+  explicit SplitMix(uint64_t seed) : s(seed) {}
+  uint64_t next() { s += kGamma; return mix64(s); }
+};
+
+static inline uint32_t edge_weight(uint64_t seed, uint32_t src, uint32_t dst,
+                                   uint32_t wmax) {
+  uint64_t h = mix64(seed ^ mix64((uint64_t(src) << 32) | dst) ^ 0x5851f42d4c957f2dULL);
+  return 1u + (uint32_t)(h % wmax);
+}
+
+// Draws edge e of an R-MAT stream.  Thresholds are 32-bit fixed point.
+struct RmatParams {
+  uint32_t scale;
+  uint64_t ta, tab, tabc;  // cumulative thresholds scaled to 2^32
+  uint64_t seed;
+};
+
+static inline void rmat_edge(const RmatParams &p, uint64_t e, uint32_t *src,
+                             uint32_t *dst) {
+  SplitMix rng(p.seed ^ mix64(e * kGamma + 0x2545f4914f6cdd1dULL));
+  uint32_t s = 0, d = 0;
+  uint64_t bits = 0;
+  int avail = 0;
+  for (uint32_t l = 0; l < p.scale; ++l) {
+    if (avail == 0) { bits = rng.next(); avail = 2; }
+    uint64_t u = bits & 0xffffffffULL;
+    bits >>= 32;
+    --avail;
+    uint32_t qs, qd;
+    if (u < p.ta) { qs = 0; qd = 0; }
+    else if (u < p.tab) { qs = 0; qd = 1; }
+    else if (u < p.tabc) { qs = 1; qd = 0; }
+    else { qs = 1; qd = 1; }
+    s = (s << 1) | qs;
+    d = (d << 1) | qd;
+  }
+  *src = s;
+  *dst = d;
+}
+
+static inline void er_edge(uint64_t seed, uint32_t n, uint64_t e, uint32_t *src,
+                           uint32_t *dst) {
+  SplitMix rng(seed ^ mix64(e * kGamma + 0x14057b7ef767814fULL));
+  uint64_t r = rng.next();
+  *src = (uint32_t)(((r & 0xffffffffULL) * n) >> 32);
+  *dst = (uint32_t)(((r >> 32) * n) >> 32);
+}
+
+// Builds a deduplicated CSR from an edge stream given as a functor
+// draw(e, &src, &dst) for e in [0, m0).  Edges are bucketed by the top bits of
+// the source without atomics (two passes over the stream), each bucket is
+// sorted and deduplicated, and the CSR is written in one more pass.
+template <class Draw>
+static int build_csr(uint32_t n, uint64_t m0, Draw draw, uint32_t drop_vertex,
+                     int weighted, uint32_t wmax, uint64_t wseed,
+                     sgw_graph **out) {
+  const int T = omp_get_max_threads();
+  int bbits = 0;
+  while ((1u << bbits) < n && bbits < 16) ++bbits;
+  int shift = 0;
+  while ((uint64_t(n) >> shift) > (uint64_t(1) << bbits)) ++shift;
+  const uint32_t B = 1u << bbits;
+  auto bucket_of = [&](uint32_t s) { return s >> shift; };
+
+  std::vector<uint64_t> hist(size_t(T) * B, 0);
+  const uint64_t per = (m0 + T - 1) / T;
+#pragma omp parallel num_threads(T)
+  {
+    int t = omp_get_thread_num();
+    uint64_t *h = &hist[size_t(t) * B];
+    uint64_t lo = std::min<uint64_t>(m0, per * t), hi = std::min<uint64_t>(m0, lo + per);
+    for (uint64_t e = lo; e < hi; ++e) {
+      uint32_t s, d;
+      draw(e, &s, &d);
+      if (s == d || s == drop_vertex) continue;
+      h[bucket_of(s)]++;
+    }
+  }
+  // prefix over (bucket, thread)
+  std::vector<uint64_t> bstart(B + 1, 0);
+  {
+    uint64_t acc = 0;
+    for (uint32_t b = 0; b < B; ++b) {
+      bstart[b] = acc;
+      for (int t = 0; t < T; ++t) {
+        uint64_t c = hist[size_t(t) * B + b];
+        hist[size_t(t) * B + b] = acc;
+        acc += c;
+      }
+    }
+    bstart[B] = acc;
+  }
+  const uint64_t kept = bstart[B];
+  uint64_t *pairs = (uint64_t *)host_alloc(sizeof(uint64_t) * std::max<uint64_t>(kept, 1), nullptr);
+  if (!pairs) return fail(SGW_ENOMEM, "edge pairs (%llu)", (unsigned long long)kept);
+#pragma omp parallel num_threads(T)
+  {
+    int t = omp_get_thread_num();
+    uint64_t *cur = &hist[size_t(t) * B];
+    uint64_t lo = std::min<uint64_t>(m0, per * t), hi = std::min<uint64_t>(m0, lo + per);
+    for (uint64_t e = lo; e < hi; ++e) {
+      uint32_t s, d;
+      draw(e, &s, &d);
+      if (s == d || s == drop_vertex) continue;
+      pairs[cur[bucket_of(s)]++] = (uint64_t(s) << 32) | d;
+    }
+  }
+  // sort + dedup each bucket, count rows
+  std::vector<uint64_t> bunique(B, 0);
+  std::vector<uint32_t> deg(size_t(n) + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(T)
+  for (int64_t b = 0; b < (int64_t)B; ++b) {
+    uint64_t *p = pairs + bstart[b];
+    uint64_t len = bstart[b + 1] - bstart[b];
+    std::sort(p, p + len);
+    uint64_t u = 0;
+    for (uint64_t i = 0; i < len; ++i) {
+      if (u == 0 || p[u - 1] != p[i]) p[u++] = p[i];
+    }
+    bunique[b] = u;
+    for (uint64_t i = 0; i < u; ++i) deg[p[i] >> 32]++;
+  }
+  uint64_t m = 0;
+  for (uint32_t b = 0; b < B; ++b) m += bunique[b];
+  sgw_graph *g = nullptr;
+  int st = graph_alloc(n, m, weighted, &g);
+  if (st != SGW_OK) { host_free(pairs); return st; }
+  {
+    uint64_t acc = 0;
+    for (uint32_t v = 0; v < n; ++v) { g->node_pointer[v] = (uint32_t)acc; acc += deg[v]; }
+    g->node_pointer[n] = (uint32_t)acc;
+  }
+  // bucket b's rows start at node_pointer[first source of bucket]
+#pragma omp parallel for schedule(dynamic, 1) num_threads(T)
+  for (int64_t b = 0; b < (int64_t)B; ++b) {
+    const uint64_t *p = pairs + bstart[b];
+    uint64_t u = bunique[b];
+    if (u == 0) continue;
+    uint64_t pos = g->node_pointer[p[0] >> 32];
+    if (weighted) {
+      uint32_t *ed = (uint32_t *)g->edges;
+      for (uint64_t i = 0; i < u; ++i) {
+        uint32_t s = (uint32_t)(p[i] >> 32), d = (uint32_t)p[i];
+        ed[2 * (pos + i)] = d;
+        ed[2 * (pos + i) + 1] = edge_weight(wseed, s, d, wmax);
+      }
+    } else {
+      uint32_t *ed = (uint32_t *)g->edges;
+      for (uint64_t i = 0; i < u; ++i) ed[pos + i] = (uint32_t)p[i];
+    }
+  }
+  host_free(pairs);
+  *out = g;
+  return SGW_OK;
+}
+
+static std::string extension_of(const char *path) {
+  std::string s(path);
+  size_t dot = s.find_last_of('.');
+  if (dot == std::string::npos) return "";
+  return s.substr(dot + 1);
+}
+
+static int load_binary(const char *path, int weighted, sgw_graph **out) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return fail(SGW_EIO, "cannot open %s", path);
+  uint32_t hdr[2];
+  if (fread(hdr, sizeof(uint32_t), 2, f) != 2) {
+    fclose(f);
+    return fail(SGW_EFORMAT, "%s: truncated header", path);
+  }
+  uint32_t n = hdr[0], m = hdr[1];
+  if (n == 0) { fclose(f); return fail(SGW_EFORMAT, "%s: zero vertices", path); }
+  const uint32_t esz = weighted ? 8 : 4;
+  fseek(f, 0, SEEK_END);
+  long long fsz = ftell(f);
+  long long want = 8LL + 4LL * n + (long long)m * esz;
+  if (fsz != want) {
+    fclose(f);
+    return fail(SGW_EFORMAT, "%s: size %lld, expected %lld for n=%u m=%u", path,
+                fsz, want, n, m);
+  }
+  fseek(f, 8, SEEK_SET);
+  sgw_graph *g = nullptr;
+  int st = graph_alloc(n, m, weighted, &g);
+  if (st != SGW_OK) { fclose(f); return st; }
+  size_t got = fread(g->node_pointer, sizeof(uint32_t), n, f);
+  g->node_pointer[n] = m;
+  // large sequential read in 256 MiB pieces
+  size_t total = size_t(m) * esz, done = 0;
+  char *dst = (char *)g->edges;
+  while (got == n && done < total) {
+    size_t piece = std::min(total - done, size_t(256) << 20);
+    size_t r = fread(dst + done, 1, piece, f);
+    if (r == 0) break;
+    done += r;
+  }
+  fclose(f);
+  if (got != n || done != total) {
+    sgw_graph_free(g);
+    return fail(SGW_EFORMAT, "%s: truncated body", path);
+  }
+  // validate: monotone pointers within [0, m], endpoints < n
+  int bad = 0;
+  for (uint32_t v = 0; v < n && !bad; ++v)
+    if (g->node_pointer[v] > g->node_pointer[v + 1]) bad = 1;
+  if (!bad) {
+    const uint32_t *ed = (const uint32_t *)g->edges;
+    const size_t stride = esz / 4;
+#pragma omp parallel for reduction(| : bad)
+    for (int64_t i = 0; i < (int64_t)m; ++i)
+      if (ed[size_t(i) * stride] >= n) bad |= 2;
+  }
+  if (bad) {
+    sgw_graph_free(g);
+    return fail(SGW_EFORMAT, "%s: %s", path,
+                bad == 1 ? "node pointers not monotone" : "edge endpoint out of range");
+  }
+  *out = g;
+  return SGW_OK;
+}
+
+static int load_text(const char *path, int weighted, sgw_graph **out) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return fail(SGW_EIO, "cannot open %s", path);
+  std::vector<uint32_t> src, dst, w;
+  char line[512];
+  uint64_t max_id = 0;
+  bool any = false;
+  while (fgets(line, sizeof(line), f)) {
+    char *p = line;
+    while (*p == ' ' || *p == '\t') ++p;
+    if (*p == '\n' || *p == '\r' || *p == 0 || *p == '#' || *p == '%') continue;
+    char *e1 = nullptr, *e2 = nullptr, *e3 = nullptr;
+    unsigned long long s = strtoull(p, &e1, 10);
+    if (e1 == p) { fclose(f); return fail(SGW_EFORMAT, "%s: bad line '%s'", path, line); }
+    unsigned long long d = strtoull(e1, &e2, 10);
+    if (e2 == e1) { fclose(f); return fail(SGW_EFORMAT, "%s: bad line '%s'", path, line); }
+    unsigned long long ww = 0;
+    if (weighted) {
+      ww = strtoull(e2, &e3, 10);
+      if (e3 == e2) { fclose(f); return fail(SGW_EFORMAT, "%s: missing weight in '%s'", path, line); }
+    }
+    if (s >= 0xffffffffULL || d >= 0xffffffffULL || ww > 0xffffffffULL) {
+      fclose(f);
+      return fail(SGW_ERANGE, "%s: value out of u32 range", path);
+    }
+    src.push_back((uint32_t)s);
+    dst.push_back((uint32_t)d);
+    if (weighted) w.push_back((uint32_t)ww);
+    max_id = std::max<uint64_t>(max_id, std::max(s, d));
+    any = true;
+  }
+  fclose(f);
+  if (!any) return fail(SGW_EFORMAT, "%s: no edges", path);
+  uint32_t n = (uint32_t)(max_id + 1);  // num_nodes = max + 1 (graph.cu:85)
+  uint64_t m = src.size();
+  sgw_graph *g = nullptr;
+  int st = graph_alloc(n, m, weighted, &g);
+  if (st != SGW_OK) return st;
+  // stable counting sort by source: file order within a row (graph.cu:92-113)
+  std::vector<uint32_t> cur(size_t(n) + 1, 0);
+  for (uint64_t i = 0; i < m; ++i) cur[src[i]]++;
+  uint32_t acc = 0;
+  for (uint32_t v = 0; v < n; ++v) { g->node_pointer[v] = acc; uint32_t c = cur[v]; cur[v] = acc; acc += c; }
+  g->node_pointer[n] = acc;
+  uint32_t *ed = (uint32_t *)g->edges;
+  for (uint64_t i = 0; i < m; ++i) {
+    uint32_t pos = cur[src[i]]++;
+    if (weighted) { ed[2 * size_t(pos)] = dst[i]; ed[2 * size_t(pos) + 1] = w[i]; }
+    else ed[pos] = dst[i];
+  }
+  *out = g;
+  return SGW_OK;
+}
+
+}  // namespace sgw
+
+using namespace sgw;
+
+extern "C" {
+
+const char *sgw_strerror(int status) {
+  switch (status) {
+    case SGW_OK: return "ok";
+    case SGW_EINVAL: return "invalid argument";
+    case SGW_EIO: return "i/o error";
+    case SGW_EFORMAT: return "unsupported or malformed graph file";
+    case SGW_ENOMEM: return "out of host memory";
+    case SGW_EBUDGET: return "device-memory budget too small";
+    case SGW_ECUDA: return "CUDA error";
+    case SGW_ETIMEOUT: return "bounded device wait timed out";
+    case SGW_ESTATE: return "wrong engine state";
+    case SGW_ERANGE: return "size out of range";
+    default: return "unknown status";
+  }
+}
+
+const char *sgw_last_error(void) { return g_err; }
+
+int sgw_graph_load(const char *path, sgw_graph **out) {
+  clear_error();
+  if (!path || !out) return fail(SGW_EINVAL, "null argument");
+  *out = nullptr;
+  std::string ext = extension_of(path);
+  if (ext == "bcsr") return load_binary(path, 0, out);
+  if (ext == "bwcsr") return load_binary(path, 1, out);
+  if (ext == "el") return load_text(path, 0, out);
+  if (ext == "wel") return load_text(path, 1, out);
+  return fail(SGW_EFORMAT, "The graph format is not supported: '%s'", path);
+}
+
+int sgw_graph_from_csr(uint32_t n, uint32_t m, const uint32_t *node_pointer,
+                       const void *edges, int weighted, sgw_graph **out) {
+  clear_error();
+  if (!out || !node_pointer || (m > 0 && !edges) || n == 0)
+    return fail(SGW_EINVAL, "null argument or zero vertices");
+  if (node_pointer[n] != m) return fail(SGW_EINVAL, "node_pointer[n] != m");
+  // the device kernels index vertex arrays by edge endpoint: validate once
+  int bad = 0;
+  for (uint32_t v = 0; v < n && !bad; ++v)
+    if (node_pointer[v] > node_pointer[v + 1]) bad = 1;
+  const uint32_t *ed = (const uint32_t *)edges;
+  const size_t stride = weighted ? 2 : 1;
+#pragma omp parallel for reduction(| : bad)
+  for (int64_t i = 0; i < (int64_t)m; ++i)
+    if (ed[size_t(i) * stride] >= n) bad |= 2;
+  if (bad)
+    return fail(SGW_EINVAL, "%s", bad & 1 ? "node_pointer not monotone" : "edge endpoint >= n");
+  sgw_graph *g = new (std::nothrow) sgw_graph();
+  if (!g) return fail(SGW_ENOMEM, "graph object");
+  g->n = n;
+  g->m = m;
+  g->weighted = weighted ? 1 : 0;
+  g->esz = weighted ? 8 : 4;
+  g->node_pointer = const_cast<uint32_t *>(node_pointer);
+  g->edges = const_cast<void *>(edges);
+  g->owns = false;
+  *out = g;
+  return SGW_OK;
+}
+
+int sgw_graph_info(const sgw_graph *g, uint32_t *n, uint32_t *m, int *weighted) {
+  if (!g) return fail(SGW_EINVAL, "null graph");
+  if (n) *n = g->n;
+  if (m) *m = g->m;
+  if (weighted) *weighted = g->weighted;
+  return SGW_OK;
+}
+
+const uint32_t *sgw_graph_node_pointer(const sgw_graph *g) { return g ? g->node_pointer : nullptr; }
+const void *sgw_graph_edges(const sgw_graph *g) { return g ? g->edges : nullptr; }
+
+int sgw_graph_out_degree(const sgw_graph *g, uint32_t *out_degree) {
+  if (!g || !out_degree) return fail(SGW_EINVAL, "null argument");
+#pragma omp parallel for
+  for (int64_t v = 0; v < (int64_t)g->n; ++v)
+    out_degree[v] = g->node_pointer[v + 1] - g->node_pointer[v];
+  return SGW_OK;
+}
+
+int sgw_graph_save(const sgw_graph *g, const char *path) {
+  clear_error();
+  if (!g || !path) return fail(SGW_EINVAL, "null argument");
+  std::string ext = extension_of(path);
+  bool bin = (ext == "bcsr" || ext == "bwcsr");
+  bool txt = (ext == "el" || ext == "wel");
+  if (!bin && !txt) return fail(SGW_EFORMAT, "unsupported extension for %s", path);
+  bool want_w = (ext == "bwcsr" || ext == "wel");
+  if (want_w && !g->weighted)
+    return fail(SGW_EINVAL, "%s needs a weighted graph", path);
+  FILE *f = fopen(path, "wb");
+  if (!f) return fail(SGW_EIO, "cannot create %s", path);
+  bool ok = true;
+  const uint32_t *ed = (const uint32_t *)g->edges;
+  const size_t stride = g->esz / 4;
+  if (bin) {
+    uint32_t hdr[2] = {g->n, g->m};
+    ok = fwrite(hdr, 4, 2, f) == 2 && fwrite(g->node_pointer, 4, g->n, f) == g->n;
+    if (ok && want_w == (bool)g->weighted) {
+      size_t total = size_t(g->m) * g->esz, done = 0;
+      while (ok && done < total) {
+        size_t piece = std::min(total - done, size_t(256) << 20);
+        ok = fwrite((const char *)g->edges + done, 1, piece, f) == piece;
+        done += piece;
+      }
+    } else if (ok) {  // unweighted file from a weighted graph: ends only
+      std::vector<uint32_t> buf;
+      buf.reserve(1 << 20);
+      for (size_t i = 0; ok && i < g->m; ++i) {
+        buf.push_back(ed[i * stride]);
+        if (buf.size() == (1u << 20) || i + 1 == g->m) {
+          ok = fwrite(buf.data(), 4, buf.size(), f) == buf.size();
+          buf.clear();
+        }
+      }
+    }
+  } else {
+    for (uint32_t v = 0; ok && v < g->n; ++v)
+      for (uint32_t i = g->node_pointer[v]; ok && i < g->node_pointer[v + 1]; ++i) {
+        if (want_w) ok = fprintf(f, "%u %u %u\n", v, ed[size_t(i) * stride], ed[size_t(i) * stride + 1]) > 0;
+        else ok = fprintf(f, "%u %u\n", v, ed[size_t(i) * stride]) > 0;
+      }
+  }
+  if (fclose(f) != 0) ok = false;
+  return ok ? SGW_OK : fail(SGW_EIO, "write failed for %s", path);
+}
+
+void sgw_graph_free(sgw_graph *g) {
+  if (!g) return;
+  if (g->owns) {
+    host_free(g->node_pointer);
+    host_free(g->edges);
+  }
+  delete g;
+}
+
+int sgw_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b,
+                 double c, uint64_t seed, int weighted, uint32_t wmax,
+                 sgw_graph **out) {
+  clear_error();
+  if (!out || scale == 0 || scale > 31 || edge_factor == 0 || a < 0 || b < 0 ||
+      c < 0 || a + b + c > 1.0 || (weighted && wmax == 0))
+    return fail(SGW_EINVAL, "bad R-MAT parameters");
+  RmatParams p;
+  p.scale = scale;
+  const double two32 = 4294967296.0;
+  p.ta = (uint64_t)(a * two32);
+  p.tab = (uint64_t)((a + b) * two32);
+  p.tabc = (uint64_t)((a + b + c) * two32);
+  p.seed = mix64(seed ^ 0x6a09e667f3bcc909ULL);
+  uint32_t n = 1u << scale;
+  uint64_t m0 = uint64_t(edge_factor) << scale;
+  uint32_t drop = n >= 2 ? n - 2 : 0xffffffffu;
+  return build_csr(n, m0, [&](uint64_t e, uint32_t *s, uint32_t *d) { rmat_edge(p, e, s, d); },
+                   drop, weighted, wmax, mix64(seed ^ 0xbb67ae8584caa73bULL), out);
+}
+
+int sgw_gen_er(uint32_t n, uint64_t m, uint64_t seed, int weighted,
+               uint32_t wmax, sgw_graph **out) {
+  clear_error();
+  if (!out || n < 2 || (weighted && wmax == 0)) return fail(SGW_EINVAL, "bad ER parameters");
+  uint64_t s2 = mix64(seed ^ 0x3c6ef372fe94f82bULL);
+  return build_csr(n, m, [&](uint64_t e, uint32_t *s, uint32_t *d) { er_edge(s2, n, e, s, d); },
+                   n - 2, weighted, wmax, mix64(seed ^ 0xbb67ae8584caa73bULL), out);
+}
+
+int sgw_graph_symmetrize(const sgw_graph *g, sgw_graph **out) {
+  clear_error();
+  if (!g || !out) return fail(SGW_EINVAL, "null argument");
+  if (g->weighted) return fail(SGW_EINVAL, "symmetrize expects an unweighted graph");
+  const uint32_t *ed = (const uint32_t *)g->edges;
+  const uint32_t n = g->n;
+  // edge e < m is the forward edge, e >= m the reverse of edge e - m
+  std::vector<uint32_t> srcof(g->m);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < (int64_t)n; ++v)
+    for (uint32_t i = g->node_pointer[v]; i < g->node_pointer[v + 1]; ++i) srcof[i] = (uint32_t)v;
+  const uint64_t m = g->m;
+  // vertex n-2 keeps no out-edges, as in the generators
+  return build_csr(n, 2 * m,
+                   [&](uint64_t e, uint32_t *s, uint32_t *d) {
+                     if (e < m) { *s = srcof[e]; *d = ed[e]; }
+                     else { *s = ed[e - m]; *d = srcof[e - m]; }
+                   },
+                   n >= 2 ? n - 2 : 0xffffffffu, 0, 1, 0, out);
+}
+
+static uint32_t uf_find(std::atomic<uint32_t> *par, uint32_t x) {
+  while (true) {
+    uint32_t p = par[x].load(std::memory_order_relaxed);
+    if (p == x) return x;
+    uint32_t gp = par[p].load(std::memory_order_relaxed);
+    if (gp != p) par[x].compare_exchange_weak(p, gp, std::memory_order_relaxed);
+    x = gp;
+  }
+}
+
+static void wcc_labels(const sgw_graph *g, std::vector<uint32_t> &root) {
+  const uint32_t n = g->n;
+  const uint32_t *ed = (const uint32_t *)g->edges;
+  const size_t stride = g->esz / 4;
+  std::atomic<uint32_t> *par = new std::atomic<uint32_t>[n];
+#pragma omp parallel for
+  for (int64_t v = 0; v < (int64_t)n; ++v) par[v].store((uint32_t)v, std::memory_order_relaxed);
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t v = 0; v < (int64_t)n; ++v) {
+    for (uint32_t i = g->node_pointer[v]; i < g->node_pointer[v + 1]; ++i) {
+      uint32_t a = (uint32_t)v, b = ed[size_t(i) * stride];
+      while (true) {
+        a = uf_find(par, a);
+        b = uf_find(par, b);
+        if (a == b) break;
+        if (a < b) std::swap(a, b);  // link the larger root under the smaller
+        uint32_t exp = a;
+        if (par[a].compare_exchange_strong(exp, b, std::memory_order_relaxed)) break;
+      }
+    }
+  }
+  root.resize(n);
+#pragma omp parallel for
+  for (int64_t v = 0; v < (int64_t)n; ++v) root[v] = uf_find(par, (uint32_t)v);
+  delete[] par;
+}
+
+int sgw_largest_wcc(const sgw_graph *g, uint32_t *vertices, uint64_t *edges) {
+  clear_error();
+  if (!g) return fail(SGW_EINVAL, "null graph");
+  std::vector<uint32_t> root;
+  wcc_labels(g, root);
+  std::vector<uint32_t> size(g->n, 0);
+  std::vector<uint64_t> esum(g->n, 0);
+  for (uint32_t v = 0; v < g->n; ++v) {
+    size[root[v]]++;
+    esum[root[v]] += g->node_pointer[v + 1] - g->node_pointer[v];
+  }
+  uint32_t best = 0;
+  for (uint32_t v = 1; v < g->n; ++v)
+    if (size[v] > size[best]) best = v;
+  if (vertices) *vertices = size[best];
+  if (edges) *edges = esum[best];
+  return SGW_OK;
+}
+
+int sgw_pick_sources(const sgw_graph *g, uint32_t count, uint64_t seed, uint32_t *out) {
+  clear_error();
+  if (!g || (!out && count)) return fail(SGW_EINVAL, "null argument");
+  std::vector<uint32_t> root;
+  wcc_labels(g, root);
+  std::vector<uint32_t> size(g->n, 0);
+  for (uint32_t v = 0; v < g->n; ++v) size[root[v]]++;
+  uint32_t best = 0;
+  for (uint32_t v = 1; v < g->n; ++v)
+    if (size[v] > size[best]) best = v;
+  std::vector<uint32_t> cand;
+  for (uint32_t v = 0; v < g->n; ++v)
+    if (root[v] == best && g->node_pointer[v + 1] > g->node_pointer[v]) cand.push_back(v);
+  if (cand.empty()) return fail(SGW_EINVAL, "no vertex with out-edges");
+  SplitMix rng(mix64(seed ^ 0xa54ff53a5f1d36f1ULL));
+  std::vector<uint32_t> chosen;
+  for (uint32_t k = 0; k < count; ++k) {
+    uint32_t v;
+    int tries = 0;
+    do {
+      v = cand[(uint32_t)(((rng.next() >> 32) * cand.size()) >> 32)];
+    } while (count <= cand.size() && ++tries < 1000 &&
+             std::find(chosen.begin(), chosen.end(), v) != chosen.end());
+    chosen.push_back(v);
+    out[k] = v;
+  }
+  return SGW_OK;
+}
+
+int sgw_plan_partitions(const uint32_t *ptr, uint32_t count, uint64_t cap,
+                        uint32_t *from_node, uint32_t *node_size,
+                        uint32_t capacity, uint32_t *num_partitions) {
+  clear_error();
+  if (!ptr || !num_partitions || cap == 0) return fail(SGW_EINVAL, "bad arguments");
+  uint32_t p = 0, from = 0;
+  while (from < count) {
+    uint32_t to = plan_next(ptr, from, count, cap);
+    if (p < capacity) {
+      if (from_node) from_node[p] = from;
+      if (node_size) node_size[p] = to - from;
+    }
+    ++p;
+    from = to;
+  }
+  *num_partitions = p;
+  if (p > capacity) return fail(SGW_ERANGE, "%u partitions exceed capacity %u", p, capacity);
+  return SGW_OK;
+}
+
+}  // extern "C"

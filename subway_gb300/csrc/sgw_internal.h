@@ -1,0 +1,52 @@
+// Internal definitions shared by the host (g++) and device (nvcc) halves of
+// libsubwaygb.  Not part of the public ABI.
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "subway_gb300.h"
+
+struct sgw_graph {
+  uint32_t n = 0;
+  uint32_t m = 0;
+  int weighted = 0;
+  uint32_t esz = 4;               // bytes per edge record (4 or 8)
+  uint32_t *node_pointer = nullptr;  // n + 1 entries, node_pointer[n] == m
+  void *edges = nullptr;          // m * esz bytes, page aligned when owned
+  bool owns = false;              // arrays allocated (and freed) by the library
+  size_t edges_bytes_alloc = 0;   // rounded allocation size of edges
+};
+
+namespace sgw {
+
+// Records a status with a message for sgw_last_error() and returns it.
+int fail(int status, const char *fmt, ...);
+void clear_error();
+
+// Page-aligned host allocation (64 KiB granularity, the GPU machine's page size),
+// suitable for cudaHostRegister.  Returns nullptr on failure.
+void *host_alloc(size_t bytes, size_t *rounded);
+void host_free(void *p);
+
+// Creates a graph object owning freshly allocated arrays.
+int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out);
+
+// Greedy partition planner shared by the host entry point and the device
+// planner: largest prefix of the queue starting at `from` whose edge count
+// is <= cap, at least one vertex.
+inline uint32_t plan_next(const uint32_t *ptr, uint32_t from, uint32_t count,
+                          uint64_t cap) {
+  // upper_bound over ptr[from+1 .. count] for ptr[from] + cap
+  uint64_t limit = (uint64_t)ptr[from] + cap;
+  uint32_t lo = from + 1, hi = count + 1;  // search in [lo, hi)
+  while (lo < hi) {
+    uint32_t mid = lo + (hi - lo) / 2;
+    if ((uint64_t)ptr[mid] <= limit) lo = mid + 1; else hi = mid;
+  }
+  uint32_t to = lo - 1;          // last index with ptr[to] - ptr[from] <= cap
+  if (to <= from) to = from + 1; // one vertex larger than cap: its own run
+  return to;
+}
+
+}  // namespace sgw

@@ -1,0 +1,669 @@
+// Device kernels of the engine (sm_103a).
+//
+// Hot path per global iteration (reference: shared/subgraph_generator.cu:
+// 128-204 and subway/*-{sync,async}.cu):
+//   k_generate   activeness + single-pass decoupled-lookback scan + compaction
+//                into the active queue (replaces prePrefix, thrust::reduce,
+//                two thrust::exclusive_scan, makeQueue, makeActiveNodesPointer)
+//   k_plan       greedy partition boundaries on the device (Partitioner)
+//   k_gather     active-edge gather from mapped pinned host CSR into an HBM
+//                edge buffer (replaces the host std::thread copy dynamic<E>)
+//   k_relax_tile CTA-cooperative expansion of a tile of frontier sources
+//                staged in shared memory (bfs/sssp/sswp/cc kernels, sync and
+//                async forms)
+//   k_relax_chunks warp-per-chunk expansion of high-degree sources
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sgw_internal.h"
+
+namespace sgw {
+
+constexpr uint32_t kInf = 4294967294u;  // DIST_INFINITY (shared/globals.hpp:27)
+
+// ---- device control block -------------------------------------------------
+struct Ctl {
+  uint32_t tile_ticket;      // dynamic tile index of the running scan
+  uint32_t tile_done;        // finished tiles of the running scan
+  uint32_t error;            // nonzero: a bounded wait gave up
+  uint32_t num_active;       // queued vertices (degree > 0) of the last generate
+  unsigned long long num_active_edges;
+  uint32_t num_parts;        // partitions of the last plan
+  uint32_t num_seen;         // vertices found active (any degree)
+  uint32_t upd[4];           // async inner iteration k: relaxations that improved
+  uint32_t wl_count[4];      // chunk-list items of inner iteration k
+  uint32_t iters_run;        // inner iterations that did work
+  uint32_t hub_active;       // single-vertex partition: the source was dirty
+  uint32_t hub_value;        // single-vertex partition: its value
+  uint32_t pad0;
+  unsigned long long reached_edges;
+  unsigned long long relaxed_edges;
+};
+
+struct Part {                // one partition of the active queue
+  uint32_t from;             // first queue index
+  uint32_t size;             // queue entries
+  uint32_t edge_from;        // ptr[from]
+  uint32_t first_vertex;     // queue[from]
+  unsigned long long edge_count;
+};
+
+struct WorkItem {            // a chunk of one high-degree source's edges
+  uint32_t boff;             // first edge in the device edge buffer
+  uint32_t count;            // edges in this chunk
+  uint32_t value;            // source value snapshot
+  uint32_t vertex;
+};
+
+// ---- small PTX helpers ----------------------------------------------------
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Warp-inclusive scan of a u32.
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x, int lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  return x;
+}
+
+// Bounded wait on a scan tile flag; returns the flag, or 0 after the limit
+// (and records the error).  Flags are (epoch << 2) | status, status 1 =
+// aggregate available, 2 = inclusive prefix available.
+constexpr uint32_t kSpinLimit = 1u << 22;
+__device__ __forceinline__ uint32_t wait_tile_flag(const uint32_t *flag, uint32_t epoch, Ctl *ctl) {
+  for (uint32_t spin = 0; spin < kSpinLimit; ++spin) {
+    uint32_t f = ld_acquire_u32(flag);
+    if ((f >> 2) == epoch && (f & 3u) != 0) return f;
+    __nanosleep(spin < 64 ? 32 : 256);
+  }
+  atomicExch(&ctl->error, 1u);
+  return 0;
+}
+
+// Decoupled look-back for tile `tile` with aggregate `agg`, run by one thread.
+// Values are packed (count << 32) | edges; both sums stay below 2^32 so the
+// packed add never carries.  Returns the exclusive prefix of the tile.
+__device__ __forceinline__ unsigned long long lookback(
+    uint32_t tile, unsigned long long agg, uint32_t *tflag,
+    unsigned long long *tagg, unsigned long long *tincl, uint32_t epoch, Ctl *ctl) {
+  if (tile == 0) {
+    st_relaxed_u64(&tincl[0], agg);
+    st_release_u32(&tflag[0], (epoch << 2) | 2u);
+    return 0ull;
+  }
+  st_relaxed_u64(&tagg[tile], agg);
+  st_release_u32(&tflag[tile], (epoch << 2) | 1u);
+  unsigned long long excl = 0;
+  int32_t j = (int32_t)tile - 1;
+  while (j >= 0) {
+    uint32_t f = wait_tile_flag(&tflag[j], epoch, ctl);
+    if (f == 0) break;  // timed out: error recorded, prefix is garbage
+    if ((f & 3u) == 2u) { excl += ld_relaxed_u64(&tincl[j]); break; }
+    excl += ld_relaxed_u64(&tagg[j]);
+    --j;
+  }
+  st_relaxed_u64(&tincl[tile], excl + agg);
+  st_release_u32(&tflag[tile], (epoch << 2) | 2u);
+  return excl;
+}
+
+// ---- generate: activeness -> scan -> compaction --------------------------
+constexpr int kGenThreads = 256;
+constexpr int kGenRounds = 16;
+constexpr uint32_t kGenTile = kGenThreads * kGenRounds;  // 4096 vertices
+
+struct GenArgs {
+  uint32_t n;
+  uint8_t *l1;
+  uint8_t *l2;
+  const uint32_t *off;       // n + 1 node pointers (device copy)
+  uint32_t *queue;           // activeNodes
+  uint32_t *ptr;             // activeNodesPointer (count + 1)
+  uint32_t *tflag;
+  unsigned long long *tagg;
+  unsigned long long *tincl;
+  Ctl *ctl;
+  uint32_t epoch;
+  uint32_t num_tiles;
+  int consume;               // sync: labels of queued vertices are cleared
+};
+
+// One CTA per 4096-vertex tile.  Each warp owns 512 consecutive vertices,
+// 32 per round: a lane reads label1|label2 of its vertex, the warp ballots the
+// activeness, and only active lanes read their node pointers to get degrees.
+// Active vertices of degree 0 have nothing to relax: their labels are
+// cleared here and they are not queued.
+__global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
+  __shared__ uint32_t s_tile;
+  __shared__ unsigned long long s_warp[kGenThreads / 32];
+  __shared__ unsigned long long s_prefix;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(&a.ctl->tile_ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  if (tile >= a.num_tiles) {  // stale ticket counter: refuse to index past the tiles
+    if (tid == 0) atomicExch(&a.ctl->error, 4u);
+    return;
+  }
+  const uint32_t wbase = tile * kGenTile + warp * (32 * kGenRounds);
+
+  uint32_t deg[kGenRounds];
+  uint32_t keepmask[kGenRounds];
+  uint32_t wcount = 0, wedges = 0, seen = 0;
+#pragma unroll
+  for (int r = 0; r < kGenRounds; ++r) {
+    const uint32_t v = wbase + r * 32 + lane;
+    bool act = false;
+    uint32_t d = 0;
+    if (v < a.n) {
+      act = (a.l1[v] | a.l2[v]) != 0;
+      if (act) {
+        d = __ldg(&a.off[v + 1]) - __ldg(&a.off[v]);
+        if (a.consume || d == 0) { a.l1[v] = 0; a.l2[v] = 0; }
+      }
+    }
+    seen += __popc(__ballot_sync(0xffffffffu, act));
+    const bool keep = act && d > 0;
+    keepmask[r] = __ballot_sync(0xffffffffu, keep);
+    deg[r] = keep ? d : 0;
+    wcount += __popc(keepmask[r]);
+    wedges += __reduce_add_sync(0xffffffffu, deg[r]);
+  }
+  if (lane == 0) {
+    s_warp[warp] = ((unsigned long long)wcount << 32) | wedges;
+    if (seen) atomicAdd(&a.ctl->num_seen, seen);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long acc = 0;
+#pragma unroll
+    for (int w = 0; w < kGenThreads / 32; ++w) {
+      unsigned long long x = s_warp[w];
+      s_warp[w] = acc;
+      acc += x;
+    }
+    const unsigned long long excl =
+        lookback(tile, acc, a.tflag, a.tagg, a.tincl, a.epoch, a.ctl);
+    s_prefix = excl;
+    if (tile == a.num_tiles - 1) {
+      const unsigned long long tot = excl + acc;
+      const uint32_t cnt = (uint32_t)(tot >> 32);
+      a.ctl->num_active = cnt;
+      a.ctl->num_active_edges = tot & 0xffffffffull;
+      a.ptr[cnt] = (uint32_t)(tot & 0xffffffffull);  // sentinel (subgraph_generator.cu:160)
+    }
+  }
+  __syncthreads();
+  unsigned long long run = s_prefix + s_warp[warp];
+  const uint32_t lt = lanemask_lt();
+#pragma unroll
+  for (int r = 0; r < kGenRounds; ++r) {
+    const uint32_t incl = warp_incl_scan(deg[r], lane);
+    const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+    if (keepmask[r] & (1u << lane)) {
+      const uint32_t pos = (uint32_t)(run >> 32) + __popc(keepmask[r] & lt);
+      a.queue[pos] = wbase + r * 32 + lane;
+      a.ptr[pos] = (uint32_t)(run & 0xffffffffull) + (incl - deg[r]);
+    }
+    run += ((unsigned long long)__popc(keepmask[r]) << 32) | tot;
+  }
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(&a.ctl->tile_done, 1u) == a.num_tiles - 1) {
+      a.ctl->tile_ticket = 0;
+      a.ctl->tile_done = 0;
+    }
+  }
+}
+
+// ---- partition planner ------------------------------------------------------
+// One warp.  For each partition: the largest run of queue entries starting at
+// `from` whose edges fit `cap`, found by a 32-way search (each step probes 32
+// evenly spaced entries and keeps the bracket of the last one that fits).
+__global__ void k_plan(const uint32_t *ptr, const uint32_t *queue, Ctl *ctl,
+                       Part *parts, uint32_t max_parts, unsigned long long cap) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t count = ctl->num_active;
+  uint32_t from = 0, p = 0;
+  while (from < count) {
+    const unsigned long long limit = (unsigned long long)ptr[from] + cap;
+    // answer t in [from, count]: largest index with ptr[t] <= limit
+    uint32_t lo = from + 1, hi = count;  // candidates above `from`
+    uint32_t best = from;
+    while (lo <= hi) {
+      const uint32_t span = hi - lo + 1;
+      const uint32_t step = (span + 31) / 32;
+      const uint32_t idx = lo + (uint32_t)lane * step;
+      const bool ok = idx <= hi && (unsigned long long)ptr[idx] <= limit;
+      const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+      const int k = __popc(bal);  // ok is a prefix of the lanes
+      if (k == 0) break;
+      const uint32_t last_ok = lo + (uint32_t)(k - 1) * step;
+      best = last_ok;
+      if (step == 1) break;
+      lo = last_ok + 1;
+      const uint32_t next_bad = lo - 1 + step;  // first probe that failed
+      if (k < 32 && next_bad - 1 < hi) hi = next_bad - 1;
+    }
+    uint32_t to = best > from ? best : from + 1;  // a vertex beyond cap runs alone
+    if (lane == 0 && p < max_parts) {
+      Part q;
+      q.from = from;
+      q.size = to - from;
+      q.edge_from = ptr[from];
+      q.first_vertex = queue[from];
+      q.edge_count = (unsigned long long)ptr[to] - ptr[from];
+      parts[p] = q;
+    }
+    ++p;
+    from = to;
+  }
+  if (lane == 0) {
+    ctl->num_parts = p;
+    if (p > max_parts) atomicExch(&ctl->error, 2u);
+  }
+}
+
+// ---- gather: host CSR -> device edge buffer -------------------------------
+constexpr int kGatherThreads = 256;
+constexpr uint32_t kGatherTile = 2048;  // output edges per CTA tile
+
+// Index of the last element <= x in a[0..len) (a non-decreasing, a[0] <= x).
+__device__ __forceinline__ uint32_t last_le(const uint32_t *a, uint32_t len, uint32_t x) {
+  uint32_t lo = 0, hi = len;  // first index with a[i] > x in [lo, hi)
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] <= x) lo = mid + 1; else hi = mid;
+  }
+  return lo - 1;
+}
+
+// Copies the edges of queue entries [from, from+size) from the mapped host
+// CSR to buf[0 .. edge_count).  Output positions are balanced per CTA; each
+// CTA stages the (buffer offset, host offset) of the sources its tile covers
+// in shared memory and every thread copies edges by binary search in it.
+// Consecutive threads read consecutive host edges of one source, so host
+// reads are coalesced; E is the edge record (one or two u32 words).
+template <int W>
+__global__ void __launch_bounds__(kGatherThreads) k_gather(
+    const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
+    const uint32_t *__restrict__ off, const uint32_t *__restrict__ host_edges,
+    uint32_t *__restrict__ buf, uint32_t from, uint32_t size, uint32_t edge_from,
+    uint32_t edge_count) {
+  __shared__ uint32_t s_bpos[kGatherTile + 1];
+  __shared__ uint32_t s_hpos[kGatherTile + 1];
+  __shared__ uint32_t s_first, s_nsrc;
+  const uint32_t ntiles = (edge_count + kGatherTile - 1) / kGatherTile;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t j0 = t * kGatherTile;
+    const uint32_t j1 = min(edge_count, j0 + kGatherTile);
+    if (threadIdx.x == 0) {
+      // sources covering [j0, j1): queue indices i with ptr[i]-edge_from in range
+      uint32_t lo = from, hi = from + size;  // last i with ptr[i]-edge_from <= j0
+      while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (ptr[mid] - edge_from <= j0) lo = mid; else hi = mid;
+      }
+      uint32_t first = lo;
+      lo = first; hi = from + size;  // last i with ptr[i]-edge_from <= j1-1
+      while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (ptr[mid] - edge_from <= j1 - 1) lo = mid; else hi = mid;
+      }
+      s_first = first;
+      s_nsrc = lo - first + 1;
+    }
+    __syncthreads();
+    const uint32_t first = s_first, nsrc = s_nsrc;
+    for (uint32_t k = threadIdx.x; k < nsrc; k += blockDim.x) {
+      const uint32_t i = first + k;
+      s_bpos[k] = ptr[i] - edge_from;
+      s_hpos[k] = off[queue[i]];
+    }
+    __syncthreads();
+    for (uint32_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+      const uint32_t k = last_le(s_bpos, nsrc, j);
+      const size_t h = (size_t)s_hpos[k] + (j - s_bpos[k]);
+      if (W == 1) {
+        buf[j] = host_edges[h];
+      } else {
+        const uint2 e = reinterpret_cast<const uint2 *>(host_edges)[h];
+        reinterpret_cast<uint2 *>(buf)[j] = e;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---- relaxation ----------------------------------------------------------------
+// Per-algorithm semiring (shared/gpu_kernels.cu): candidate value from the
+// source value and the edge, and whether it improves the destination.
+template <int ALGO> struct Op;
+template <> struct Op<SGW_BFS> {   // bfs_kernel: value+1, atomicMin (:45-46)
+  static constexpr bool kMax = false;
+  __device__ static uint32_t cand(uint32_t v, uint32_t) { return v + 1; }
+};
+template <> struct Op<SGW_SSSP> {  // sssp_kernel: value+w8, atomicMin (:146-149)
+  static constexpr bool kMax = false;
+  __device__ static uint32_t cand(uint32_t v, uint32_t w) { return v + w; }
+};
+template <> struct Op<SGW_SSWP> {  // sswp_kernel: min(value,w8), atomicMax (:196-199)
+  static constexpr bool kMax = true;
+  __device__ static uint32_t cand(uint32_t v, uint32_t w) { return min(v, w); }
+};
+template <> struct Op<SGW_CC> {    // cc_kernel: value, atomicMin (:96-98)
+  static constexpr bool kMax = false;
+  __device__ static uint32_t cand(uint32_t v, uint32_t) { return v; }
+};
+
+// Relaxes one edge; returns true if the destination improved.
+template <int ALGO>
+__device__ __forceinline__ bool relax_edge(uint32_t sval, uint32_t dst, uint32_t w,
+                                           uint32_t *value, uint8_t *nxt) {
+  const uint32_t c = Op<ALGO>::cand(sval, w);
+  const uint32_t cur = value[dst];
+  if (Op<ALGO>::kMax ? (c > cur) : (c < cur)) {
+    const uint32_t old = Op<ALGO>::kMax ? atomicMax(&value[dst], c) : atomicMin(&value[dst], c);
+    if (Op<ALGO>::kMax ? (c > old) : (c < old)) {
+      nxt[dst] = 1;
+      return true;
+    }
+  }
+  return false;
+}
+
+// Whether a source with this value may push (guards u32 overflow of INF+w;
+// the reference relies on INF vertices never carrying a label).
+template <int ALGO>
+__device__ __forceinline__ bool can_push(uint32_t v) {
+  if (ALGO == SGW_BFS || ALGO == SGW_SSSP) return v != kInf;
+  if (ALGO == SGW_SSWP) return v != 0;
+  return true;
+}
+
+struct RelaxArgs {
+  const uint32_t *queue;
+  const uint32_t *ptr;
+  const uint32_t *buf;       // device edge buffer (W words per edge)
+  uint32_t *value;
+  uint8_t *cur;              // async: label of this inner iteration (cleared)
+  uint8_t *nxt;              // label set on improvement
+  Ctl *ctl;
+  WorkItem *wl;
+  uint32_t wl_cap;
+  uint32_t from, size, edge_from;
+  uint32_t iter;             // inner iteration number (1-based)
+  uint32_t tile_degree_max;  // sources above this go to the chunk list
+  uint32_t chunk_edges;
+};
+
+constexpr int kRelaxThreads = 256;
+
+// Tile of kRelaxThreads partition sources per CTA (grid-stride).  Each thread
+// claims one source (async: only if its label is set, clearing it), the CTA
+// scans the degrees in shared memory and all threads expand the tile's edges
+// together: edge j of the tile belongs to the source found by binary search
+// in the scanned degrees.  Sources above tile_degree_max are cut into chunks
+// and appended to the chunk list instead.
+template <int ALGO, bool ASYNC, int W>
+__global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
+  __shared__ uint32_t s_scan[kRelaxThreads + 1];
+  __shared__ uint32_t s_boff[kRelaxThreads];
+  __shared__ uint32_t s_val[kRelaxThreads];
+  __shared__ uint32_t s_hub[kRelaxThreads];
+  __shared__ uint32_t s_nhub, s_wbase;
+  __shared__ int s_skip;
+  const int tid = threadIdx.x;
+  const uint32_t slot = a.iter & 3u;
+  if (tid == 0) {
+    int skip = 0;
+    if (ASYNC && a.iter > 1 && ld_acquire_u32(&a.ctl->upd[(a.iter - 1) & 3u]) == 0) skip = 1;
+    s_skip = skip;
+    if (blockIdx.x == 0) {
+      a.ctl->upd[(a.iter + 1) & 3u] = 0;
+      a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
+      if (!skip) atomicAdd(&a.ctl->iters_run, 1u);
+    }
+  }
+  __syncthreads();
+  if (s_skip) return;
+  bool any_update = false;
+  const uint32_t ntiles = (a.size + kRelaxThreads - 1) / kRelaxThreads;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    if (tid == 0) s_nhub = 0;
+    __syncthreads();
+    const uint32_t i = a.from + t * kRelaxThreads + tid;
+    uint32_t d = 0, boff = 0, val = 0, u = 0;
+    if (i < a.from + a.size) {
+      u = a.queue[i];
+      bool act = true;
+      if (ASYNC) {
+        act = a.cur[u] != 0;
+        if (act) a.cur[u] = 0;
+      }
+      if (act) {
+        val = a.value[u];
+        if (can_push<ALGO>(val)) {
+          const uint32_t p0 = a.ptr[i];
+          d = a.ptr[i + 1] - p0;
+          boff = p0 - a.edge_from;
+          if (d > a.tile_degree_max) {
+            s_hub[atomicAdd(&s_nhub, 1u)] = tid;
+          }
+        }
+      }
+    }
+    s_boff[tid] = boff;
+    s_val[tid] = val;
+    __syncthreads();
+    // chunk out high-degree sources (whole CTA writes the items)
+    const uint32_t nhub = s_nhub;
+    for (uint32_t h = 0; h < nhub; ++h) {
+      const uint32_t ht = s_hub[h];
+      if (tid == ht) {
+        const uint32_t nch = (d + a.chunk_edges - 1) / a.chunk_edges;
+        s_wbase = atomicAdd(&a.ctl->wl_count[slot], nch);
+        s_scan[kRelaxThreads] = d;  // temporary: degree of this hub
+      }
+      __syncthreads();
+      const uint32_t hd = s_scan[kRelaxThreads];
+      const uint32_t nch = (hd + a.chunk_edges - 1) / a.chunk_edges;
+      const uint32_t wb = s_wbase;
+      for (uint32_t c = tid; c < nch; c += blockDim.x) {
+        if (wb + c < a.wl_cap) {
+          WorkItem it;
+          it.boff = s_boff[ht] + c * a.chunk_edges;
+          it.count = min(a.chunk_edges, hd - c * a.chunk_edges);
+          it.value = s_val[ht];
+          it.vertex = 0;
+          a.wl[wb + c] = it;
+        } else {
+          atomicExch(&a.ctl->error, 3u);
+        }
+      }
+      __syncthreads();
+    }
+    if (d > a.tile_degree_max) d = 0;
+    // block exclusive scan of d
+    {
+      const int lane = tid & 31, warp = tid >> 5;
+      const uint32_t incl = warp_incl_scan(d, lane);
+      __shared__ uint32_t s_wsum[kRelaxThreads / 32];
+      if (lane == 31) s_wsum[warp] = incl;
+      __syncthreads();
+      if (tid == 0) {
+        uint32_t acc = 0;
+        for (int w = 0; w < kRelaxThreads / 32; ++w) { uint32_t x = s_wsum[w]; s_wsum[w] = acc; acc += x; }
+        s_scan[kRelaxThreads] = acc;
+      }
+      __syncthreads();
+      s_scan[tid] = s_wsum[warp] + incl - d;
+      __syncthreads();
+    }
+    const uint32_t total = s_scan[kRelaxThreads];
+    for (uint32_t j = tid; j < total; j += blockDim.x) {
+      // last source k with s_scan[k] <= j (sources with d == 0 share offsets;
+      // the last one with that offset is the one that owns edge j)
+      uint32_t lo = 0, hi = kRelaxThreads;
+      while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (s_scan[mid] <= j) lo = mid + 1; else hi = mid;
+      }
+      const uint32_t k = lo - 1;
+      const uint32_t e = s_boff[k] + (j - s_scan[k]);
+      uint32_t dst, w = 0;
+      if (W == 1) {
+        dst = a.buf[e];
+      } else {
+        const uint2 ed = reinterpret_cast<const uint2 *>(a.buf)[e];
+        dst = ed.x;
+        w = ed.y;
+      }
+      any_update |= relax_edge<ALGO>(s_val[k], dst, w, a.value, a.nxt);
+    }
+    __syncthreads();
+  }
+  if (__syncthreads_or(any_update) && tid == 0) atomicAdd(&a.ctl->upd[slot], 1u);
+}
+
+// Chunk list of inner iteration `iter`: one warp per item.
+template <int ALGO, bool ASYNC, int W>
+__global__ void __launch_bounds__(kRelaxThreads) k_relax_chunks(RelaxArgs a) {
+  const uint32_t slot = a.iter & 3u;
+  if (ASYNC && a.iter > 1 && ld_acquire_u32(&a.ctl->upd[(a.iter - 1) & 3u]) == 0) return;
+  const uint32_t items = min(ld_acquire_u32(&a.ctl->wl_count[slot]), a.wl_cap);
+  const int lane = threadIdx.x & 31;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  bool any_update = false;
+  for (uint32_t it = gw; it < items; it += nw) {
+    const WorkItem wi = a.wl[it];
+    for (uint32_t j = lane; j < wi.count; j += 32) {
+      const uint32_t e = wi.boff + j;
+      uint32_t dst, w = 0;
+      if (W == 1) {
+        dst = a.buf[e];
+      } else {
+        const uint2 ed = reinterpret_cast<const uint2 *>(a.buf)[e];
+        dst = ed.x;
+        w = ed.y;
+      }
+      any_update |= relax_edge<ALGO>(wi.value, dst, w, a.value, a.nxt);
+    }
+  }
+  if (__syncthreads_or(any_update) && threadIdx.x == 0) atomicAdd(&a.ctl->upd[slot], 1u);
+}
+
+// Single-vertex partition (degree above the edge buffer): claim the source
+// once, then relax its edges piece by piece.
+template <bool ASYNC>
+__global__ void k_hub_claim(uint32_t u, const uint32_t *value, uint8_t *l1, uint8_t *l2, Ctl *ctl) {
+  uint32_t act = 1;
+  if (ASYNC) {
+    act = (l1[u] | l2[u]) != 0;
+    l1[u] = 0;
+    l2[u] = 0;
+  }
+  ctl->hub_active = act;
+  ctl->hub_value = value[u];
+  ctl->upd[1] = 0;
+}
+
+template <int ALGO, int W>
+__global__ void k_relax_flat(const uint32_t *buf, uint32_t count, uint32_t *value,
+                             uint8_t *nxt, Ctl *ctl) {
+  if (!ctl->hub_active) return;
+  const uint32_t sval = ctl->hub_value;
+  if (!can_push<ALGO>(sval)) return;
+  bool any = false;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+    uint32_t dst, w = 0;
+    if (W == 1) dst = buf[j];
+    else { const uint2 ed = reinterpret_cast<const uint2 *>(buf)[j]; dst = ed.x; w = ed.y; }
+    any |= relax_edge<ALGO>(sval, dst, w, value, nxt);
+  }
+  if (__syncthreads_or(any) && threadIdx.x == 0) atomicAdd(&ctl->upd[1], 1u);
+}
+
+// ---- label hand-off (shared/gpu_kernels.cu:515-534) ------------------------
+// mixLabels: label1 |= label2; label2 = 0 for the partition's sources.
+__global__ void k_mix(const uint32_t *queue, uint32_t from, uint32_t size, uint8_t *l1, uint8_t *l2) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < size; i += gridDim.x * blockDim.x) {
+    const uint32_t u = queue[from + i];
+    if (l2[u]) { l1[u] = 1; l2[u] = 0; }
+  }
+}
+
+// ---- state init and summaries ------------------------------------------------
+// Initial values and labels of subway/<algo>-<mode>.cu.
+__global__ void k_init(uint32_t n, int algo, int mode, uint32_t source, uint32_t *value,
+                       uint8_t *l1, uint8_t *l2) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    uint32_t val;
+    switch (algo) {
+      case SGW_BFS:
+      case SGW_SSSP: val = (v == source) ? 0u : kInf; break;
+      case SGW_SSWP: val = (v == source) ? kInf : 0u; break;
+      default: val = v; break;  // CC
+    }
+    value[v] = val;
+    uint8_t a1, a2;
+    if (mode == SGW_ASYNC) { a1 = 1; a2 = 0; }            // all active for the first generate
+    else if (algo == SGW_CC) { a1 = 0; a2 = 1; }           // cc-sync.cu:31-33
+    else { a1 = 0; a2 = (v == source) ? 1 : 0; }           // bfs-sync.cu:30-36
+    l1[v] = a1;
+    l2[v] = a2;
+  }
+}
+
+// After the first async generate, label1 = {source} (subway/sssp-async.cu:59-63);
+// cc-async keeps every vertex active.
+__global__ void k_async_reset(uint32_t n, uint32_t source, uint8_t *l1) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    l1[v] = (v == source) ? 1 : 0;
+}
+
+// Graph500 m_reached: edges whose source left its initial value.
+__global__ void k_reached(uint32_t n, int algo, uint32_t source, const uint32_t *value,
+                          const uint32_t *off, Ctl *ctl) {
+  unsigned long long acc = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const uint32_t x = value[v];
+    bool reached;
+    switch (algo) {
+      case SGW_BFS:
+      case SGW_SSSP: reached = x != kInf; break;
+      case SGW_SSWP: reached = x != 0 || v == source; break;
+      default: reached = true; break;
+    }
+    if (reached) acc += off[v + 1] - off[v];
+  }
+  acc = __reduce_add_sync(0xffffffffu, (uint32_t)acc) ; // per-warp (degree sums fit u32 per warp)
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&ctl->reached_edges, acc);
+}
+
+}  // namespace sgw

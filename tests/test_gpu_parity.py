@@ -1,0 +1,146 @@
+"""Parity of the CUDA engine against the CPU oracle (bit-exact for the
+integer algorithms), through the C ABI, on seeded graphs small enough for the
+serial oracle, across budgets that force one or hundreds of partitions."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ALGS = ["bfs", "sssp", "sswp", "cc"]
+MODES = ["sync", "async"]
+
+
+def _graph(native, scale, weighted, seed=11, ef=16):
+    return native.Graph.rmat(scale, ef, seed=seed, weighted=weighted, wmax=64)
+
+
+def _oracle(orc, g, algo, src):
+    e = g.edges
+    if algo in ("bfs", "cc") and g.weighted:
+        e = np.ascontiguousarray(e[:, 0])
+    return orc.run(algo, g.node_pointer, e, src)
+
+
+@pytest.fixture(scope="module")
+def g12w(gpu):
+    return _graph(gpu, 12, True)
+
+
+@pytest.fixture(scope="module")
+def g12u(gpu):
+    return _graph(gpu, 12, False)
+
+
+@pytest.mark.parametrize("algo", ALGS)
+@pytest.mark.parametrize("mode", MODES)
+def test_in_memory_small(gpu, orc, g12w, g12u, algo, mode):
+    g = g12w if algo in ("sssp", "sswp") else g12u
+    eng = gpu.Engine(g)
+    src = 0
+    vals, st = eng.run(algo, mode, src)
+    ref = _oracle(orc, g, algo, src)
+    assert np.array_equal(vals, ref), f"{algo}-{mode}: {np.count_nonzero(vals != ref)} mismatches"
+    assert st["global_iterations"] >= 1
+
+
+@pytest.mark.parametrize("algo", ALGS)
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("budget_edges", [64, 1000, 20000])
+def test_out_of_budget(gpu, orc, g12w, algo, mode, budget_edges):
+    """Budgets far below the graph: many partitions, hubs split over pieces."""
+    g = g12w
+    fixed = 18 * g.n + 72 * 1024
+    eng = gpu.Engine(g, budget_bytes=fixed + budget_edges * 2 * 8 + 4096)
+    cap = eng.max_partition_size()
+    assert cap < g.m
+    src = int(g.pick_sources(1, seed=3)[0])
+    vals, st = eng.run(algo, mode, src)
+    ref = _oracle(orc, g, algo, src)
+    assert np.array_equal(vals, ref), f"{algo}-{mode} cap={cap}: {np.count_nonzero(vals != ref)} mismatches"
+    assert eng.device_bytes() <= fixed + budget_edges * 2 * 8 + 4096
+    assert st["partitions"] >= st["global_iterations"]
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_config1_rmat16(gpu, orc, mode):
+    """RMAT 2^16, edge factor 16, source 0, BFS and SSSP (w in [1,64])."""
+    gw = _graph(gpu, 16, True, seed=1)
+    gu = _graph(gpu, 16, False, seed=1)
+    for algo, g in (("bfs", gu), ("sssp", gw)):
+        eng = gpu.Engine(g)
+        vals, _ = eng.run(algo, mode, 0)
+        assert np.array_equal(vals, _oracle(orc, g, algo, 0)), f"{algo}-{mode}"
+
+
+@pytest.mark.parametrize("algo", ["bfs", "sssp"])
+def test_many_sources_er(gpu, orc, algo):
+    g = gpu.Graph.er(5000, 60000, seed=9, weighted=(algo == "sssp"))
+    eng = gpu.Engine(g, budget_bytes=18 * g.n + 72 * 1024 + 3000 * 16)
+    for src in g.pick_sources(4, seed=2):
+        for mode in MODES:
+            vals, _ = eng.run(algo, mode, int(src))
+            assert np.array_equal(vals, _oracle(orc, g, algo, int(src))), (algo, mode, src)
+
+
+def test_generate_matches_reference_compaction(gpu, orc, g12u):
+    """The first sync generate from a CC start (all vertices active) equals
+    the reference's compaction restricted to vertices with out-edges."""
+    g = g12u
+    eng = gpu.Engine(g)
+    eng.state_init("cc", "sync")
+    nodes, ptr = eng.read_active()
+    deg = g.out_degree()
+    q, p = orc.generate(np.zeros(g.n, np.uint8), np.ones(g.n, np.uint8), deg)
+    keep = deg[q] > 0
+    assert np.array_equal(nodes, q[keep])
+    assert np.array_equal(ptr[:-1], p[:-1][keep])
+    assert ptr[-1] == p[-1]
+
+
+def test_step_api_loop(gpu, orc, g12w):
+    """The reference's app loop written against the step API."""
+    g = g12w
+    eng = gpu.Engine(g, budget_bytes=18 * g.n + 72 * 1024 + 5000 * 16)
+    eng.state_init("sssp", "async", 0)
+    iters = 0
+    while True:
+        parts = eng.partition()
+        if not parts:
+            break
+        iters += 1
+        for i in range(len(parts)):
+            assert eng.process_partition(i) >= 1
+        a, _ = eng.generate()
+        if a == 0:
+            break
+    vals = eng.read_values()
+    assert np.array_equal(vals, _oracle(orc, g, "sssp", 0))
+    assert iters >= 1
+
+
+def test_hub_larger_than_budget(gpu, orc):
+    """A vertex whose out-degree exceeds the edge buffer (the reference's
+    partitioner never terminates here) is streamed in pieces."""
+    n = 3000
+    rng = np.random.default_rng(5)
+    src = np.concatenate([np.zeros(2500, np.int64), rng.integers(0, n, 4000)])
+    dst = np.concatenate([np.arange(1, 2501), rng.integers(0, n, 4000)])
+    keep = (src != dst) & (src != n - 2)
+    src, dst = src[keep], dst[keep]
+    order = np.lexsort((dst, src))
+    src, dst = src[order], dst[order]
+    pairs = np.unique(np.stack([src, dst], 1), axis=0)
+    src, dst = pairs[:, 0], pairs[:, 1]
+    npt = np.zeros(n + 1, np.uint32)
+    np.add.at(npt, src + 1, 1)
+    npt = np.cumsum(npt).astype(np.uint32)
+    w = (1 + (src * 7 + dst * 13) % 50).astype(np.uint32)
+    edges = np.stack([dst.astype(np.uint32), w], 1)
+    g = gpu.Graph.from_csr(npt, edges, True)
+    eng = gpu.Engine(g, budget_bytes=18 * n + 72 * 1024 + 500 * 16)
+    assert eng.max_partition_size() < 2500
+    for algo in ("bfs", "sssp", "sswp", "cc"):
+        for mode in MODES:
+            vals, _ = eng.run(algo, mode, 0)
+            ref = _oracle(orc, g, algo, 0)
+            assert np.array_equal(vals, ref), (algo, mode)

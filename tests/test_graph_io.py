@@ -1,0 +1,140 @@
+"""Graph formats and the seeded generators (CPU only)."""
+import hashlib
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+README_EL = "0 1\n0 3\n2 3\n1 2\n"            # the example graph of the reference README
+README_WEL = "0 1 26\n0 3 33\n2 3 40\n1 2 10\n"
+
+
+def _digest(g):
+    h = hashlib.sha256()
+    h.update(g.node_pointer.tobytes())
+    h.update(np.ascontiguousarray(g.edges).tobytes())
+    return h.hexdigest()
+
+
+def test_rmat_deterministic(native):
+    a = native.Graph.rmat(12, 8, seed=3, weighted=True)
+    b = native.Graph.rmat(12, 8, seed=3, weighted=True)
+    c = native.Graph.rmat(12, 8, seed=4, weighted=True)
+    assert _digest(a) == _digest(b) != _digest(c)
+
+
+def test_rmat_independent_of_thread_count(native):
+    code = ("import sys; sys.path.insert(0, %r); from subway_gb300 import native as N; "
+            "import hashlib, numpy as np; g=N.Graph.rmat(13, 8, seed=9, weighted=True); "
+            "h=hashlib.sha256(); h.update(g.node_pointer.tobytes()); "
+            "h.update(np.ascontiguousarray(g.edges).tobytes()); print(h.hexdigest())" % str(ROOT))
+    outs = []
+    for t in ("1", "3"):
+        env = dict(os.environ, OMP_NUM_THREADS=t)
+        outs.append(subprocess.run([sys.executable, "-c", code], env=env, capture_output=True,
+                                   text=True, check=True).stdout.strip())
+    assert outs[0] == outs[1]
+
+
+@pytest.mark.parametrize("kind", ["rmat", "er"])
+def test_generator_invariants(native, kind):
+    g = (native.Graph.rmat(12, 16, seed=2, weighted=True, wmax=64) if kind == "rmat"
+         else native.Graph.er(4096, 60000, seed=2, weighted=True, wmax=64))
+    npt, e = g.node_pointer, g.edges
+    assert npt[0] == 0 and npt[-1] == g.m and np.all(np.diff(npt.astype(np.int64)) >= 0)
+    src = np.repeat(np.arange(g.n, dtype=np.uint32), np.diff(npt))
+    assert np.all(src != e[:, 0]), "self-loop"
+    key = src.astype(np.uint64) << np.uint64(32) | e[:, 0].astype(np.uint64)
+    assert np.all(np.diff(key.astype(np.int64)) > 0), "rows unsorted or duplicated"
+    assert e[:, 1].min() >= 1 and e[:, 1].max() <= 64
+    assert npt[g.n - 1] == npt[g.n - 2], "vertex n-2 must have no out-edges"
+
+
+def test_rmat_skew(native):
+    g = native.Graph.rmat(14, 16, seed=1)
+    deg = g.out_degree()
+    assert deg[0] == deg.max(), "vertex 0 is the top hub (no permutation)"
+    assert g.m > 0.7 * 16 * g.n
+
+
+@pytest.mark.parametrize("ext", ["bcsr", "bwcsr", "el", "wel"])
+def test_save_load_round_trip(native, tmp_path, ext):
+    g = native.Graph.rmat(10, 8, seed=5, weighted=ext in ("bwcsr", "wel"))
+    p = tmp_path / f"g.{ext}"
+    g.save(p)
+    h = native.Graph.load(p)
+    assert h.weighted == g.weighted
+    if ext in ("el", "wel"):
+        # text drops trailing isolated vertices: n = max id + 1 (graph.cu:85)
+        assert h.m == g.m and h.n <= g.n
+        assert np.array_equal(h.node_pointer, g.node_pointer[: h.n + 1])
+    else:
+        assert (h.n, h.m) == (g.n, g.m)
+        assert np.array_equal(h.node_pointer, g.node_pointer)
+    assert np.array_equal(h.edges, g.edges)
+
+
+def test_readme_example(native, tmp_path):
+    (tmp_path / "Graph.el").write_text(README_EL)
+    (tmp_path / "Graph.wel").write_text(README_WEL)
+    g = native.Graph.load(tmp_path / "Graph.el")
+    assert (g.n, g.m) == (4, 4)
+    assert g.node_pointer.tolist() == [0, 2, 3, 4, 4]
+    assert g.ends.tolist() == [1, 3, 2, 3]
+    w = native.Graph.load(tmp_path / "Graph.wel")
+    assert w.edges.tolist() == [[1, 26], [3, 33], [2, 10], [3, 40]]
+    # the converter's binary output, written by this library, reads back
+    w.save(tmp_path / "Graph.bwcsr")
+    raw = (tmp_path / "Graph.bwcsr").read_bytes()
+    assert np.frombuffer(raw[:8], np.uint32).tolist() == [4, 4]
+    assert len(raw) == 8 + 4 * 4 + 4 * 8
+
+
+def test_format_errors(native, tmp_path):
+    with pytest.raises(native.SgwError) as e:
+        native.Graph.load(tmp_path / "missing.bcsr")
+    assert e.value.status == -2
+    (tmp_path / "g.txt").write_text(README_EL)
+    with pytest.raises(native.SgwError) as e:
+        native.Graph.load(tmp_path / "g.txt")
+    assert e.value.status == -3
+    g = native.Graph.rmat(8, 4, seed=1)
+    g.save(tmp_path / "t.bcsr")
+    raw = (tmp_path / "t.bcsr").read_bytes()
+    (tmp_path / "trunc.bcsr").write_bytes(raw[:-4])
+    with pytest.raises(native.SgwError) as e:
+        native.Graph.load(tmp_path / "trunc.bcsr")
+    assert e.value.status == -3
+    bad = bytearray(raw)
+    bad[-4:] = np.uint32(10**6).tobytes()  # endpoint out of range
+    (tmp_path / "bad.bcsr").write_bytes(bytes(bad))
+    with pytest.raises(native.SgwError):
+        native.Graph.load(tmp_path / "bad.bcsr")
+    (tmp_path / "w.wel").write_text("0 1\n")
+    with pytest.raises(native.SgwError):
+        native.Graph.load(tmp_path / "w.wel")
+
+
+def test_symmetrize(native):
+    g = native.Graph.rmat(11, 8, seed=4)
+    s = g.symmetrize()
+    npt, e = s.node_pointer, s.ends
+    src = np.repeat(np.arange(s.n), np.diff(npt))
+    fwd = set(zip(src.tolist(), e.tolist()))
+    for u, v in list(fwd)[:5000]:
+        assert (v, u) in fwd or v == s.n - 2
+    assert np.all(np.diff(npt)[s.n - 2] == 0)
+
+
+def test_pick_sources(native):
+    g = native.Graph.rmat(12, 16, seed=6)
+    a = g.pick_sources(8, seed=1)
+    b = g.pick_sources(8, seed=1)
+    assert np.array_equal(a, b) and len(set(a.tolist())) == 8
+    assert np.all(g.out_degree()[a] > 0)
+    nv, ne = g.largest_wcc()
+    assert nv > g.n // 4 and ne > g.m // 2
