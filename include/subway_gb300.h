@@ -102,7 +102,8 @@ typedef struct sgw_engine_opts {
   uint32_t inner_batch;    /* async inner iterations launched per host check  */
   uint32_t tile_degree_max;/* sources above this degree go to the chunk list  */
   uint32_t chunk_edges;    /* edges per chunk-list item (multiple of 32)      */
-  uint32_t reserved[8];
+  uint32_t gather_ctas;    /* CTAs of the gather kernel, 0 = 2 per SM          */
+  uint32_t reserved[7];
 } sgw_engine_opts;
 
 void sgw_engine_opts_default(sgw_engine_opts *opts);
@@ -155,7 +156,9 @@ typedef struct sgw_run_stats {
   uint64_t gather_launches;
   uint64_t relax_launches;
   uint64_t generate_launches;
-  uint64_t reserved[4];
+  uint64_t relaxed_edges;       /* edges expanded by the relaxation kernels     */
+  uint64_t relaxed_sources;     /* sources whose edges were expanded            */
+  uint64_t reserved[2];
 } sgw_run_stats;
 
 /* One whole application run: the init loops, the first generate, the
@@ -197,6 +200,32 @@ int sgw_read_active(sgw_engine *e, uint32_t *nodes, uint32_t *ptr,
 /* Statistics accumulated since the last sgw_state_init / sgw_run. */
 int sgw_get_stats(const sgw_engine *e, sgw_run_stats *stats);
 
+/* ---- per-partition trace ----------------------------------------------
+ * One record per processed partition.  The reference prints the inner
+ * iteration count of each async partition (subway/sssp-async.cu:117); the
+ * trace carries that and the transfer volume, and is the training data of
+ * the learned scheduler. */
+typedef struct sgw_trace_rec {
+  uint32_t global_iteration;      /* 1-based                                  */
+  uint32_t partition;             /* index within the global iteration        */
+  uint32_t num_partitions;        /* partitions in this global iteration      */
+  uint32_t inner_iterations;      /* relaxation passes run on the partition   */
+  uint32_t active_nodes;          /* queued vertices of the partition         */
+  uint32_t first_vertex;          /* lowest vertex id of the partition        */
+  uint64_t active_edges;          /* edges of those vertices                  */
+  uint64_t iteration_active_nodes;/* queued vertices of the whole iteration   */
+  uint64_t iteration_active_edges;
+  uint64_t bytes_h2d;             /* bytes read from host for the partition   */
+  uint32_t transfer;              /* 0 compacted gather, 1 range stream, 2 split vertex */
+  uint32_t reserved;
+} sgw_trace_rec;
+
+/* Records are kept from the next sgw_state_init / sgw_run on while enabled. */
+int sgw_trace_enable(sgw_engine *e, int on);
+int sgw_trace_count(const sgw_engine *e, uint64_t *count);
+int sgw_trace_read(const sgw_engine *e, sgw_trace_rec *out, uint64_t capacity,
+                   uint64_t *count);
+
 /* Partition planning on the host: the greedy split of a compacted active
  * queue (prefix array ptr of count+1 entries) into runs whose edge count is
  * at most cap; a vertex with more than cap edges gets a run of its own.
@@ -210,6 +239,12 @@ int sgw_plan_partitions(const uint32_t *ptr, uint32_t count, uint64_t cap,
 
 /* Number of CUDA devices visible (0 on a machine without a GPU). */
 int sgw_device_count(int *count);
+
+/* Host-link copy bandwidth of `device` in GB/s: pinned host -> device and
+ * device -> host cudaMemcpyAsync of `bytes`, best of `iters` (the
+ * denominator of the gather kernel's roofline). */
+int sgw_probe_link(int device, uint64_t bytes, int iters, double *h2d_gbs,
+                   double *d2h_gbs);
 
 #ifdef __cplusplus
 }

@@ -88,7 +88,10 @@ struct sgw_engine {
   uint64_t num_active_edges = 0;
   uint32_t num_parts = 0;
   bool parts_valid = false;
+  uint32_t gitr = 0;  // current global iteration (1-based once processing)
   sgw_run_stats stats{};
+  bool trace_on = false;
+  std::vector<sgw_trace_rec> trace;
 };
 
 namespace {
@@ -283,6 +286,25 @@ int generate_and_plan(sgw_engine *e, int consume) {
 
 bool is_hub(const sgw_engine *e, const Part &p) { return p.edge_count > e->cap; }
 
+void trace_partition(sgw_engine *e, uint32_t p, uint32_t inner) {
+  if (!e->trace_on) return;
+  const Part &q = e->h_parts[p];
+  sgw_trace_rec r;
+  memset(&r, 0, sizeof(r));
+  r.global_iteration = e->gitr;
+  r.partition = p;
+  r.num_partitions = e->num_parts;
+  r.inner_iterations = inner;
+  r.active_nodes = q.size;
+  r.first_vertex = q.first_vertex;
+  r.active_edges = q.edge_count;
+  r.iteration_active_nodes = e->num_active;
+  r.iteration_active_edges = e->num_active_edges;
+  r.bytes_h2d = q.edge_count * 4ull * e->W;
+  r.transfer = is_hub(e, q) ? 2 : 0;
+  e->trace.push_back(r);
+}
+
 int enqueue_gather(sgw_engine *e, uint32_t p, cudaStream_t s) {
   const Part &q = e->h_parts[p];
   const uint32_t b = p % e->nbuf;
@@ -290,7 +312,8 @@ int enqueue_gather(sgw_engine *e, uint32_t p, cudaStream_t s) {
   CK(cudaStreamWaitEvent(s, e->ev_free[b], 0));
   size_t slot = 0;
   TRY(prof_begin(e, K_GATHER, s, &slot));
-  const uint32_t grid = grid_for(e, q.edge_count, kGatherTile);
+  const uint32_t gmax = e->opts.gather_ctas ? e->opts.gather_ctas : 2u * e->num_sms;
+  const uint32_t grid = std::min<uint32_t>(grid_for(e, q.edge_count, kGatherTile), gmax);
   if (e->W == 1)
     k_gather<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_edges,
                                                 e->d_buf[b], q.from, q.size, q.edge_from,
@@ -467,6 +490,8 @@ int state_init(sgw_engine *e, const sgw_run_params *p) {
   e->stats = sgw_run_stats{};
   e->prof_used = 0;
   e->initialized = false;
+  e->gitr = 0;
+  e->trace.clear();
   const uint32_t src = p->algo == SGW_CC ? 0xffffffffu : p->source;
   k_init<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->algo, p->mode, src, e->d_value,
                                                         e->d_l1, e->d_l2);
@@ -494,13 +519,15 @@ int process_iteration(sgw_engine *e) {
     const Part &q = e->h_parts[p];
     const uint32_t b = p % e->nbuf;
     if (e->nbuf > 1 && p + 1 < P) TRY(enqueue_gather(e, p + 1, e->s_copy));
+    uint32_t inner = 1;
     if (is_hub(e, q)) {
       TRY(process_hub(e, q, b));
     } else {
       CK(cudaStreamWaitEvent(e->s_comp, e->ev_ready[b], 0));
-      TRY(process_resident(e, q, b, nullptr));
+      TRY(process_resident(e, q, b, &inner));
     }
     CK(cudaEventRecord(e->ev_free[b], e->s_comp));
+    trace_partition(e, p, inner);
     if (e->nbuf == 1 && p + 1 < P) TRY(enqueue_gather(e, p + 1, e->s_copy));
     e->stats.partitions += 1;
   }
@@ -541,6 +568,49 @@ int sgw_device_count(int *count) {
   cudaGetLastError();
   *count = c;
   return SGW_OK;
+}
+
+int sgw_probe_link(int device, uint64_t bytes, int iters, double *h2d_gbs, double *d2h_gbs) {
+  clear_error();
+  if (bytes == 0 || iters <= 0) return fail(SGW_EINVAL, "bad probe size");
+  CK(cudaSetDevice(device));
+  void *h = nullptr, *d = nullptr;
+  cudaStream_t s = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  int st = SGW_OK;
+  double best_h2d = 0, best_d2h = 0;
+  if (cudaMallocHost(&h, bytes) != cudaSuccess || cudaMalloc(&d, bytes) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    st = fail(SGW_ECUDA, "probe allocation");
+  } else {
+    memset(h, 1, bytes);
+    for (int dir = 0; dir < 2 && st == SGW_OK; ++dir) {
+      for (int i = 0; i <= iters; ++i) {  // first copy warms up
+        cudaEventRecord(a, s);
+        if (dir == 0) cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s);
+        else cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, s);
+        cudaEventRecord(b, s);
+        if (cudaEventSynchronize(b) != cudaSuccess) { st = fail(SGW_ECUDA, "probe copy"); break; }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        double gbs = (double)bytes / (ms * 1e6);
+        if (i > 0) {
+          if (dir == 0) best_h2d = std::max(best_h2d, gbs);
+          else best_d2h = std::max(best_d2h, gbs);
+        }
+      }
+    }
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (s) cudaStreamDestroy(s);
+  if (d) cudaFree(d);
+  if (h) cudaFreeHost(h);
+  cudaGetLastError();
+  if (h2d_gbs) *h2d_gbs = best_h2d;
+  if (d2h_gbs) *d2h_gbs = best_d2h;
+  return st;
 }
 
 int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_engine **out) {
@@ -753,7 +823,29 @@ int sgw_process_partition(sgw_engine *e, uint32_t i, uint32_t *inner_iterations)
   CK(cudaStreamSynchronize(e->s_comp));
   TRY(read_ctl(e));
   e->stats.partitions += 1;
+  if (i == 0) e->gitr += 1;
+  trace_partition(e, i, iters);
   if (inner_iterations) *inner_iterations = iters;
+  return SGW_OK;
+}
+
+int sgw_trace_enable(sgw_engine *e, int on) {
+  if (!e) return fail(SGW_EINVAL, "null engine");
+  e->trace_on = on != 0;
+  return SGW_OK;
+}
+
+int sgw_trace_count(const sgw_engine *e, uint64_t *count) {
+  if (!e || !count) return fail(SGW_EINVAL, "null argument");
+  *count = e->trace.size();
+  return SGW_OK;
+}
+
+int sgw_trace_read(const sgw_engine *e, sgw_trace_rec *out, uint64_t capacity, uint64_t *count) {
+  if (!e || !count) return fail(SGW_EINVAL, "null argument");
+  uint64_t k = std::min<uint64_t>(capacity, e->trace.size());
+  if (out && k) memcpy(out, e->trace.data(), k * sizeof(sgw_trace_rec));
+  *count = k;
   return SGW_OK;
 }
 
@@ -804,6 +896,7 @@ int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values, sgw_run_st
   uint32_t gitr = 0;
   while (e->num_active > 0) {
     ++gitr;
+    e->gitr = gitr;
     e->stats.active_vertices += e->num_active;
     e->stats.active_edges += e->num_active_edges;
     TRY(process_iteration(e));
@@ -823,6 +916,8 @@ int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values, sgw_run_st
   CK(cudaStreamSynchronize(e->s_comp));
   TRY(check_ctl_error(e));
   e->stats.reached_edges = e->h_ctl->reached_edges;
+  e->stats.relaxed_edges = e->h_ctl->relaxed_edges;
+  e->stats.relaxed_sources = e->h_ctl->relaxed_sources;
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, e->ev_t0, e->ev_t1));
   e->stats.ms_device = ms;

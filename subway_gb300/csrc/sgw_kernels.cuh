@@ -40,6 +40,7 @@ struct Ctl {
   uint32_t pad0;
   unsigned long long reached_edges;
   unsigned long long relaxed_edges;
+  unsigned long long relaxed_sources;
 };
 
 struct Part {                // one partition of the active queue
@@ -345,14 +346,28 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(
       s_hpos[k] = off[queue[i]];
     }
     __syncthreads();
-    for (uint32_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-      const uint32_t k = last_le(s_bpos, nsrc, j);
-      const size_t h = (size_t)s_hpos[k] + (j - s_bpos[k]);
-      if (W == 1) {
-        buf[j] = host_edges[h];
-      } else {
-        const uint2 e = reinterpret_cast<const uint2 *>(host_edges)[h];
-        reinterpret_cast<uint2 *>(buf)[j] = e;
+    // four independent host loads in flight per thread before any store
+    constexpr int U = 4;
+    for (uint32_t jb = j0 + threadIdx.x; jb < j1; jb += U * blockDim.x) {
+      uint2 e[U];
+      uint32_t jj[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t j = jb + u * blockDim.x;
+        jj[u] = j;
+        if (j < j1) {
+          const uint32_t k = last_le(s_bpos, nsrc, j);
+          const size_t h = (size_t)s_hpos[k] + (j - s_bpos[k]);
+          if (W == 1) e[u].x = host_edges[h];
+          else e[u] = reinterpret_cast<const uint2 *>(host_edges)[h];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (jj[u] < j1) {
+          if (W == 1) buf[jj[u]] = e[u].x;
+          else reinterpret_cast<uint2 *>(buf)[jj[u]] = e[u];
+        }
       }
     }
     __syncthreads();
@@ -473,13 +488,17 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
           boff = p0 - a.edge_from;
           if (d > a.tile_degree_max) {
             s_hub[atomicAdd(&s_nhub, 1u)] = tid;
+            atomicAdd(&a.ctl->relaxed_edges, (unsigned long long)d);
           }
         }
       }
     }
     s_boff[tid] = boff;
     s_val[tid] = val;
-    __syncthreads();
+    {
+      const int nsrc = __syncthreads_count(d > 0);
+      if (tid == 0 && nsrc) atomicAdd(&a.ctl->relaxed_sources, (unsigned long long)nsrc);
+    }
     // chunk out high-degree sources (whole CTA writes the items)
     const uint32_t nhub = s_nhub;
     for (uint32_t h = 0; h < nhub; ++h) {
@@ -525,6 +544,7 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
       __syncthreads();
     }
     const uint32_t total = s_scan[kRelaxThreads];
+    if (tid == 0 && total) atomicAdd(&a.ctl->relaxed_edges, (unsigned long long)total);
     for (uint32_t j = tid; j < total; j += blockDim.x) {
       // last source k with s_scan[k] <= j (sources with d == 0 share offsets;
       // the last one with that offset is the one that owns edge j)

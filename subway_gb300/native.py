@@ -27,7 +27,7 @@ MODES = {"sync": SYNC, "async": ASYNC}
 class EngineOpts(C.Structure):
     _fields_ = [("budget_bytes", C.c_uint64), ("device", C.c_int32), ("flags", C.c_uint32),
                 ("inner_batch", C.c_uint32), ("tile_degree_max", C.c_uint32),
-                ("chunk_edges", C.c_uint32), ("reserved", C.c_uint32 * 8)]
+                ("chunk_edges", C.c_uint32), ("gather_ctas", C.c_uint32), ("reserved", C.c_uint32 * 7)]
 
 
 class RunParams(C.Structure):
@@ -44,7 +44,8 @@ class RunStats(C.Structure):
                 ("ms_partition", C.c_double), ("ms_gather", C.c_double), ("ms_relax", C.c_double),
                 ("launches", C.c_uint64), ("gather_launches", C.c_uint64),
                 ("relax_launches", C.c_uint64), ("generate_launches", C.c_uint64),
-                ("reserved", C.c_uint64 * 4)]
+                ("relaxed_edges", C.c_uint64), ("relaxed_sources", C.c_uint64),
+                ("reserved", C.c_uint64 * 2)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -84,6 +85,10 @@ _PROTOS = {
     "sgw_get_stats": (C.c_int, [_P, C.POINTER(RunStats)]),
     "sgw_plan_partitions": (C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, C.c_uint32, _u32p]),
     "sgw_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "sgw_probe_link": (C.c_int, [C.c_int, C.c_uint64, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "sgw_trace_enable": (C.c_int, [_P, C.c_int]),
+    "sgw_trace_count": (C.c_int, [_P, _u64p]),
+    "sgw_trace_read": (C.c_int, [_P, _P, C.c_uint64, _u64p]),
     "sgw_gen_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
                                C.c_uint64, C.c_int, C.c_uint32, C.POINTER(_P)]),
     "sgw_gen_er": (C.c_int, [C.c_uint32, C.c_uint64, C.c_uint64, C.c_int, C.c_uint32, C.POINTER(_P)]),
