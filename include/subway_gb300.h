@@ -240,6 +240,35 @@ int sgw_plan_partitions(const uint32_t *ptr, uint32_t count, uint64_t cap,
 /* Number of CUDA devices visible (0 on a machine without a GPU). */
 int sgw_device_count(int *count);
 
+/* ---- allocation-free compaction ------------------------------------------
+ * No counterpart in the reference (its generate step allocates its scan
+ * buffers through thrust, shared/subgraph_generator.cu:138-150).
+ *
+ * For callers that cannot call cudaMalloc: a host framework that already owns
+ * every byte of device memory through its own pool, or a caller in a
+ * latency-critical loop where cudaMalloc/cudaFree would synchronise the
+ * device.  It runs the engine's activeness -> scan -> compaction kernel on
+ * device arrays the caller provides (label1, label2 bytes of n vertices;
+ * node_pointer of n+1 entries; queue of n and ptr of n+1 entries), with the
+ * scan's tile state in a static device array inside this library
+ * (about 321 KB, held by every GPU that loads the library until exit).  It
+ * calls no allocating routine.
+ *  - n must be at most SGW_NOALLOC_MAX_VERTICES; larger n returns SGW_ERANGE.
+ *  - consume != 0 clears the labels of queued vertices (the sync form);
+ *    labels of active vertices with no out-edges are always cleared.
+ *  - The first call on a device looks up the static array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - Every call shares the one static array: calls whose work overlaps on
+ *    the GPU (other streams, other host threads) race; serialise them.
+ *  - stream is a cudaStream_t (NULL = legacy default stream); the call
+ *    synchronises it and returns the counts on the host. */
+#define SGW_NOALLOC_MAX_VERTICES 67108864u
+int sgw_generate_noalloc(uint8_t *d_label1, uint8_t *d_label2,
+                         const uint32_t *d_node_pointer, uint32_t n, int consume,
+                         uint32_t *d_queue, uint32_t *d_ptr, void *stream,
+                         uint32_t *num_active, uint64_t *num_active_edges);
+
 /* Host-link copy bandwidth of `device` in GB/s: pinned host -> device and
  * device -> host cudaMemcpyAsync of `bytes`, best of `iters` (the
  * denominator of the gather kernel's roofline). */

@@ -927,3 +927,92 @@ int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values, sgw_run_st
 }
 
 }  // extern "C"
+
+// ---- allocation-free compaction ---------------------------------------------
+// sgw_generate_noalloc runs the engine's generate kernel (k_generate) on
+// caller-owned device arrays, with the scan's tile state and counters in the
+// file-scope array below instead of an engine arena.  Nothing here allocates.
+//
+// Limit: SGW_NOALLOC_MAX_VERTICES vertices = 16384 scan tiles of 4096.
+// Size: 16384 x (4 B flag + 8 B aggregate + 8 B inclusive prefix) plus the
+// control block, about 321 KB, held by every GPU that loads the library.
+
+#include <mutex>
+
+namespace {
+
+constexpr uint32_t kNoAllocTiles = SGW_NOALLOC_MAX_VERTICES / kGenTile;
+constexpr size_t kNaFlagOff = 0;
+constexpr size_t kNaAggOff = kNaFlagOff + 4ull * kNoAllocTiles;
+constexpr size_t kNaInclOff = kNaAggOff + 8ull * kNoAllocTiles;
+constexpr size_t kNaCtlOff = kNaInclOff + 8ull * kNoAllocTiles;
+constexpr size_t kNoAllocBytes = kNaCtlOff + ((sizeof(Ctl) + 255) / 256) * 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[kNoAllocMaxDevices] = {};  // device address per device
+uint32_t g_noalloc_epoch[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
+extern "C" int sgw_generate_noalloc(uint8_t *d_label1, uint8_t *d_label2,
+                                    const uint32_t *d_node_pointer, uint32_t n, int consume,
+                                    uint32_t *d_queue, uint32_t *d_ptr, void *stream,
+                                    uint32_t *num_active, uint64_t *num_active_edges) {
+  clear_error();
+  if (n == 0 || n > SGW_NOALLOC_MAX_VERTICES)
+    return fail(SGW_ERANGE, "sgw_generate_noalloc: n=%u outside 1..%u (static scratch limit)", n,
+                SGW_NOALLOC_MAX_VERTICES);
+  if (!d_label1 || !d_label2 || !d_node_pointer || !d_queue || !d_ptr)
+    return fail(SGW_EINVAL, "sgw_generate_noalloc: null device pointer");
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(SGW_ERANGE, "device %d", dev);
+  unsigned char *scratch = nullptr;
+  uint32_t epoch = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {  // once per device, with that device current
+      void *p = nullptr;
+      cudaError_t ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (ce != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SGW_ECUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(ce));
+      }
+      g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    scratch = g_noalloc_ptr[dev];
+    epoch = g_noalloc_epoch[dev] = (g_noalloc_epoch[dev] + 1) & 0x3fffffffu;
+    if (epoch == 0) epoch = g_noalloc_epoch[dev] = 1;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Ctl *ctl = reinterpret_cast<Ctl *>(scratch + kNaCtlOff);
+  // the previous call's counters are not trusted: clear the control block
+  CK(cudaMemsetAsync(ctl, 0, sizeof(Ctl), s));
+  GenArgs a;
+  a.n = n;
+  a.l1 = d_label1;
+  a.l2 = d_label2;
+  a.off = d_node_pointer;
+  a.queue = d_queue;
+  a.ptr = d_ptr;
+  a.tflag = reinterpret_cast<uint32_t *>(scratch + kNaFlagOff);
+  a.tagg = reinterpret_cast<unsigned long long *>(scratch + kNaAggOff);
+  a.tincl = reinterpret_cast<unsigned long long *>(scratch + kNaInclOff);
+  a.ctl = ctl;
+  a.epoch = epoch;
+  a.num_tiles = (n + kGenTile - 1) / kGenTile;
+  a.consume = consume ? 1 : 0;
+  k_generate<<<a.num_tiles, kGenThreads, 0, s>>>(a);
+  CK(cudaGetLastError());
+  Ctl h;
+  CK(cudaMemcpyAsync(&h, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (h.error == 1) return fail(SGW_ETIMEOUT, "scan look-back wait timed out");
+  if (h.error) return fail(SGW_ESTATE, "scan error %u", h.error);
+  if (num_active) *num_active = h.num_active;
+  if (num_active_edges) *num_active_edges = h.num_active_edges;
+  return SGW_OK;
+}

@@ -86,6 +86,7 @@ _PROTOS = {
     "sgw_plan_partitions": (C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, C.c_uint32, _u32p]),
     "sgw_device_count": (C.c_int, [C.POINTER(C.c_int)]),
     "sgw_probe_link": (C.c_int, [C.c_int, C.c_uint64, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "sgw_generate_noalloc": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_int, _P, _P, _P, _u32p, _u64p]),
     "sgw_trace_enable": (C.c_int, [_P, C.c_int]),
     "sgw_trace_count": (C.c_int, [_P, _u64p]),
     "sgw_trace_read": (C.c_int, [_P, _P, C.c_uint64, _u64p]),
