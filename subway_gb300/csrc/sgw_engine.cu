@@ -65,6 +65,9 @@ struct sgw_engine {
   Part *d_parts = nullptr;
   WorkItem *d_wl = nullptr;
   uint32_t *d_buf[2] = {nullptr, nullptr};
+  double *d_pval = nullptr, *d_delta = nullptr, *d_qpush = nullptr;  // PR family
+  int fam = 0;
+  uint64_t cap_fam[2] = {0, 0};  // edge-buffer capacity of each family in this arena
   uint64_t cap = 0;  // edges per buffer
   uint32_t nbuf = 2;
   uint32_t max_parts = 0, wl_cap = 0, num_tiles = 0;
@@ -151,62 +154,91 @@ int read_ctl(sgw_engine *e) {
 }
 
 // ---- arena layout ------------------------------------------------------------------
+// One cudaMalloc holds everything.  The node pointers, scan tile state and
+// control block sit at the front for the engine's lifetime; the rest is carved
+// per run for the algorithm family:
+//   integer (BFS/SSSP/SSWP/CC): value u32, label1/label2 u8, queue, ptr
+//   PR: rank f64, residual f64, queue, ptr, per-queue-entry push f64
+// followed by the partition table, the chunk list and the edge buffers.
+enum Family { FAM_INT = 0, FAM_PR = 1 };
+
 struct Layout {
-  size_t off, value, l1, l2, queue, ptr, tflag, tagg, tincl, ctl, parts, wl, buf0, buf1, total;
+  size_t off, tflag, tagg, tincl, ctl;                // common
+  size_t value, l1, l2, queue, ptr, delta, qpush;     // family
+  size_t parts, wl, buf0, buf1, total;
   uint64_t cap;
   uint32_t max_parts, wl_cap;
 };
 
-size_t fixed_bytes(uint32_t n, uint32_t num_tiles) {
-  size_t b = 0;
-  b += align_up(4ull * (n + 1), 256);   // off
-  b += align_up(4ull * n, 256);         // value
-  b += 2 * align_up(n, 256);            // l1, l2
-  b += align_up(4ull * n, 256);         // queue
-  b += align_up(4ull * (n + 1), 256);   // ptr
-  b += align_up(4ull * num_tiles, 256) + 2 * align_up(8ull * num_tiles, 256);
-  b += align_up(sizeof(Ctl), 256);
-  return b;
-}
-
-Layout make_layout(uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf, uint32_t num_tiles,
-                   uint64_t cap, uint32_t chunk, uint32_t tdm) {
+Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
+                   uint32_t num_tiles, uint64_t cap, uint32_t chunk, uint32_t tdm) {
   Layout L{};
   size_t p = 0;
   auto take = [&](size_t bytes) { size_t at = p; p += align_up(bytes, 256); return at; };
   L.off = take(4ull * (n + 1));
-  L.value = take(4ull * n);
-  L.l1 = take(n);
-  L.l2 = take(n);
-  L.queue = take(4ull * n);
-  L.ptr = take(4ull * (n + 1));
   L.tflag = take(4ull * num_tiles);
   L.tagg = take(8ull * num_tiles);
   L.tincl = take(8ull * num_tiles);
   L.ctl = take(sizeof(Ctl));
+  if (fam == FAM_INT) {
+    L.value = take(4ull * n);
+    L.l1 = take(n);
+    L.l2 = take(n);
+  } else {
+    L.value = take(8ull * n);
+    L.delta = take(8ull * n);
+  }
+  L.queue = take(4ull * n);
+  L.ptr = take(4ull * (n + 1));
+  if (fam == FAM_PR) L.qpush = take(8ull * n);
   L.cap = cap;
-  L.max_parts = (uint32_t)std::min<uint64_t>(2ull * ((uint64_t)m / cap + 1) + 2, 0x7fffffffull);
+  L.max_parts = (uint32_t)std::min<uint64_t>(2ull * ((uint64_t)m / std::max<uint64_t>(cap, 1) + 1) + 2,
+                                             0x7fffffffull);
   L.wl_cap = (uint32_t)std::min<uint64_t>(cap / chunk + cap / std::max<uint32_t>(tdm, 1) + 64, 0x7fffffffull);
   L.parts = take(sizeof(Part) * (size_t)L.max_parts);
-  L.wl = take(sizeof(WorkItem) * (size_t)L.wl_cap);
+  L.wl = take(16ull * (size_t)L.wl_cap);  // WorkItem and PrItem are 16 B
   L.buf0 = take(cap * esz);
   L.buf1 = nbuf > 1 ? take(cap * esz) : L.buf0;
   L.total = p;
   return L;
 }
 
-int carve(sgw_engine *e, const Layout &L) {
+// Largest edge-buffer capacity whose layout fits `bytes` (0 if none does).
+uint64_t fit_cap(int fam, const sgw_engine_opts &o, uint32_t n, uint32_t m, uint32_t esz,
+                 uint32_t nbuf, uint32_t num_tiles, uint64_t bytes) {
+  const Layout L0 = make_layout(fam, n, m, esz, nbuf, num_tiles, 64, o.chunk_edges, o.tile_degree_max);
+  if (L0.total > bytes) return 0;
+  const double per_edge = (double)nbuf * esz + 16.0 / o.chunk_edges + 16.0 / o.tile_degree_max +
+                          2.0 * sizeof(Part) / 64.0;
+  uint64_t cap = (uint64_t)((double)(bytes - L0.total) / per_edge) + 64;
+  cap = std::min<uint64_t>(cap, std::max<uint64_t>(m, 64));
+  cap = std::min<uint64_t>(cap, 4294967294ull);  // max_partition_size <= DIST_INFINITY
+  while (cap > 64 && make_layout(fam, n, m, esz, nbuf, num_tiles, cap, o.chunk_edges,
+                                 o.tile_degree_max).total > bytes)
+    cap -= std::max<uint64_t>(cap / 64, 64);
+  if (cap < 64) cap = 64;
+  return make_layout(fam, n, m, esz, nbuf, num_tiles, cap, o.chunk_edges, o.tile_degree_max).total <= bytes
+             ? cap : 0;
+}
+
+int carve(sgw_engine *e, int fam, uint64_t cap) {
+  const Layout L = make_layout(fam, e->n, e->m, 4 * e->W, e->nbuf, e->num_tiles, cap,
+                               e->opts.chunk_edges, e->opts.tile_degree_max);
+  if (L.total > e->arena_bytes) return fail(SGW_EBUDGET, "layout exceeds the arena");
   char *b = e->d_arena;
   e->d_off = (uint32_t *)(b + L.off);
-  e->d_value = (uint32_t *)(b + L.value);
-  e->d_l1 = (uint8_t *)(b + L.l1);
-  e->d_l2 = (uint8_t *)(b + L.l2);
-  e->d_queue = (uint32_t *)(b + L.queue);
-  e->d_ptr = (uint32_t *)(b + L.ptr);
   e->d_tflag = (uint32_t *)(b + L.tflag);
   e->d_tagg = (unsigned long long *)(b + L.tagg);
   e->d_tincl = (unsigned long long *)(b + L.tincl);
   e->d_ctl = (Ctl *)(b + L.ctl);
+  e->d_value = (uint32_t *)(b + L.value);
+  e->d_l1 = fam == FAM_INT ? (uint8_t *)(b + L.l1) : nullptr;
+  e->d_l2 = fam == FAM_INT ? (uint8_t *)(b + L.l2) : nullptr;
+  e->d_pval = fam == FAM_PR ? (double *)(b + L.value) : nullptr;
+  e->d_delta = fam == FAM_PR ? (double *)(b + L.delta) : nullptr;
+  e->d_qpush = fam == FAM_PR ? (double *)(b + L.qpush) : nullptr;
+  e->d_queue = (uint32_t *)(b + L.queue);
+  e->d_ptr = (uint32_t *)(b + L.ptr);
   e->d_parts = (Part *)(b + L.parts);
   e->d_wl = (WorkItem *)(b + L.wl);
   e->d_buf[0] = (uint32_t *)(b + L.buf0);
@@ -214,6 +246,7 @@ int carve(sgw_engine *e, const Layout &L) {
   e->cap = L.cap;
   e->max_parts = L.max_parts;
   e->wl_cap = L.wl_cap;
+  e->fam = fam;
   return SGW_OK;
 }
 
@@ -241,10 +274,16 @@ int launch_generate(sgw_engine *e, int consume) {
   a.epoch = e->epoch;
   a.num_tiles = e->num_tiles;
   a.consume = consume;
+  a.delta = e->d_delta;
+  a.pval = e->d_pval;
+  a.qpush = e->d_qpush;
+  a.acc = (double)e->params.pr_acc;
+  a.damping = (double)e->params.pr_damping;
   CK(cudaMemsetAsync(&e->d_ctl->num_seen, 0, sizeof(uint32_t), e->s_comp));
   size_t slot = 0;
   TRY(prof_begin(e, K_GENERATE, e->s_comp, &slot));
-  k_generate<<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  if (e->fam == FAM_PR) k_generate<true><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  else k_generate<false><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
   CK(cudaGetLastError());
   TRY(prof_end(e, e->s_comp, slot));
   e->stats.launches += 1;
@@ -374,7 +413,40 @@ int relax_dispatch(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, bool
   return relax_dispatch_w<ALGO, 2>(e, q, b, iter, async, cur, nxt);
 }
 
+template <bool ASYNC, int W>
+int launch_pr_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter) {
+  PrArgs a;
+  a.queue = e->d_queue;
+  a.ptr = e->d_ptr;
+  a.buf = e->d_buf[b];
+  a.pval = e->d_pval;
+  a.delta = e->d_delta;
+  a.qpush = e->d_qpush;
+  a.ctl = e->d_ctl;
+  a.wl = reinterpret_cast<PrItem *>(e->d_wl);
+  a.wl_cap = e->wl_cap;
+  a.from = q.from;
+  a.size = q.size;
+  a.edge_from = q.edge_from;
+  a.iter = iter;
+  a.tile_degree_max = e->opts.tile_degree_max;
+  a.chunk_edges = e->opts.chunk_edges;
+  a.acc = (double)e->params.pr_acc;
+  a.damping = (double)e->params.pr_damping;
+  k_pr_tile<ASYNC, W><<<grid_for(e, q.size, kRelaxThreads), kRelaxThreads, 0, e->s_comp>>>(a);
+  CK(cudaGetLastError());
+  k_pr_chunks<ASYNC, W><<<e->num_sms * 4, kRelaxThreads, 0, e->s_comp>>>(a);
+  CK(cudaGetLastError());
+  e->stats.launches += 2;
+  e->stats.relax_launches += 2;
+  return SGW_OK;
+}
+
 int launch_relax(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, bool async) {
+  if (e->params.algo == SGW_PR) {
+    if (e->W == 1) return async ? launch_pr_pair<true, 1>(e, q, b, iter) : launch_pr_pair<false, 1>(e, q, b, iter);
+    return async ? launch_pr_pair<true, 2>(e, q, b, iter) : launch_pr_pair<false, 2>(e, q, b, iter);
+  }
   uint8_t *cur = e->d_l1, *nxt = e->d_l2;
   if (async && (iter % 2 == 0)) std::swap(cur, nxt);  // ping-pong (sssp-async.cu:108-109)
   switch (e->params.algo) {
@@ -402,8 +474,10 @@ int launch_flat(sgw_engine *e, uint32_t b, uint32_t count) {
 // and relax its edges piece by piece (one inner iteration).
 int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
   const bool async = e->params.mode == SGW_ASYNC;
+  const bool pr = e->params.algo == SGW_PR;
   const uint32_t u = q.first_vertex;
-  if (async) k_hub_claim<true><<<1, 1, 0, e->s_comp>>>(u, e->d_value, e->d_l1, e->d_l2, e->d_ctl);
+  if (pr) k_pr_hub_claim<<<1, 1, 0, e->s_comp>>>(q.from, e->d_qpush, e->d_ctl);
+  else if (async) k_hub_claim<true><<<1, 1, 0, e->s_comp>>>(u, e->d_value, e->d_l1, e->d_l2, e->d_ctl);
   else k_hub_claim<false><<<1, 1, 0, e->s_comp>>>(u, e->d_value, e->d_l1, e->d_l2, e->d_ctl);
   CK(cudaGetLastError());
   const uint64_t deg = q.edge_count;
@@ -418,8 +492,13 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
     TRY(prof_end(e, e->s_comp, slot));
     e->stats.h2d_bytes += cnt * esz;
     TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
-    int st;
+    int st = SGW_OK;
     switch (e->params.algo) {
+      case SGW_PR:
+        if (e->W == 1) k_pr_flat<1><<<grid_for(e, cnt, 256), 256, 0, e->s_comp>>>(e->d_buf[b], cnt, e->d_delta, e->d_ctl);
+        else k_pr_flat<2><<<grid_for(e, cnt, 256), 256, 0, e->s_comp>>>(e->d_buf[b], cnt, e->d_delta, e->d_ctl);
+        if (cudaGetLastError() != cudaSuccess) st = fail(SGW_ECUDA, "k_pr_flat launch");
+        break;
       case SGW_BFS: st = launch_flat<SGW_BFS>(e, b, cnt); break;
       case SGW_SSSP: st = launch_flat<SGW_SSSP>(e, b, cnt); break;
       case SGW_SSWP: st = launch_flat<SGW_SSWP>(e, b, cnt); break;
@@ -448,9 +527,11 @@ int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_o
     if (iters_out) *iters_out = 1;
     return SGW_OK;
   }
-  k_mix<<<grid_for(e, q.size, 256), 256, 0, e->s_comp>>>(e->d_queue, q.from, q.size, e->d_l1, e->d_l2);
-  CK(cudaGetLastError());
-  e->stats.launches += 1;
+  if (e->params.algo != SGW_PR) {  // PR carries no labels
+    k_mix<<<grid_for(e, q.size, 256), 256, 0, e->s_comp>>>(e->d_queue, q.from, q.size, e->d_l1, e->d_l2);
+    CK(cudaGetLastError());
+    e->stats.launches += 1;
+  }
   const uint32_t max_inner = e->params.max_inner ? e->params.max_inner : 0xffffffffu;
   uint32_t iter = 1;
   const uint32_t batch = std::max<uint32_t>(1, e->opts.inner_batch);
@@ -475,10 +556,13 @@ int validate_params(const sgw_engine *e, const sgw_run_params *p) {
   if (!p) return fail(SGW_EINVAL, "null params");
   if (p->algo < SGW_BFS || p->algo > SGW_PR) return fail(SGW_EINVAL, "bad algorithm %d", p->algo);
   if (p->mode != SGW_SYNC && p->mode != SGW_ASYNC) return fail(SGW_EINVAL, "bad mode %d", p->mode);
-  if (p->algo == SGW_PR) return fail(SGW_EINVAL, "PageRank is not available in this build");
+  if (p->algo == SGW_PR && e->cap_fam[FAM_PR] == 0)
+    return fail(SGW_EBUDGET, "budget too small for the PageRank vertex state (f64 ranks and residuals)");
+  if (p->algo == SGW_PR && !(p->pr_acc > 0.0f) )
+    return fail(SGW_EINVAL, "pr_acc must be positive");
   if ((p->algo == SGW_SSSP || p->algo == SGW_SSWP) && !e->g->weighted)
     return fail(SGW_EINVAL, "SSSP/SSWP need a weighted graph (.bwcsr/.wel)");
-  if (p->algo != SGW_CC && p->source >= e->n)
+  if (p->algo != SGW_CC && p->algo != SGW_PR && p->source >= e->n)
     return fail(SGW_EINVAL, "source %u out of range (n=%u)", p->source, e->n);
   return SGW_OK;
 }
@@ -492,15 +576,20 @@ int state_init(sgw_engine *e, const sgw_run_params *p) {
   e->initialized = false;
   e->gitr = 0;
   e->trace.clear();
-  const uint32_t src = p->algo == SGW_CC ? 0xffffffffu : p->source;
-  k_init<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->algo, p->mode, src, e->d_value,
-                                                        e->d_l1, e->d_l2);
+  const int fam = p->algo == SGW_PR ? FAM_PR : FAM_INT;
+  if (fam != e->fam) TRY(carve(e, fam, e->cap_fam[fam]));
+  const uint32_t src = (p->algo == SGW_CC || p->algo == SGW_PR) ? 0xffffffffu : p->source;
+  if (fam == FAM_PR)
+    k_pr_init<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, (double)p->pr_init, e->d_pval, e->d_delta);
+  else
+    k_init<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->algo, p->mode, src, e->d_value,
+                                                          e->d_l1, e->d_l2);
   CK(cudaGetLastError());
   CK(cudaMemsetAsync(e->d_ctl, 0, sizeof(Ctl), e->s_comp));
   e->stats.launches += 1;
   const bool async = p->mode == SGW_ASYNC;
   TRY(generate_and_plan(e, async ? 0 : 1));
-  if (async && p->algo != SGW_CC) {
+  if (async && p->algo != SGW_CC && p->algo != SGW_PR) {
     k_async_reset<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->source, e->d_l1);
     CK(cudaGetLastError());
     e->stats.launches += 1;
@@ -649,42 +738,44 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   e->num_sms = prop.multiProcessorCount;
 
   const uint32_t esz = 4 * e->W;
-  const size_t F = fixed_bytes(e->n, e->num_tiles);
-  const double per_edge = (double)e->nbuf * esz + 16.0 / o.chunk_edges + 16.0 / o.tile_degree_max;
+  // The arena never exceeds what holds the whole graph in both buffers.
+  const uint64_t mfull = std::max<uint64_t>(e->m, 64);
+  size_t need = 0;
+  for (int fam = 0; fam < 2; ++fam)
+    need = std::max(need, make_layout(fam, e->n, e->m, esz, e->nbuf, e->num_tiles, mfull,
+                                      o.chunk_edges, o.tile_degree_max).total);
   uint64_t budget = o.budget_bytes;
   if (budget == 0) {
     // Subway's rule: 0.9 * (totalGlobalMem - 32 n) bytes of edges
     // (shared/subgraph.cu:24), here on top of the engine's own vertex state.
+    const Layout L0 = make_layout(FAM_PR, e->n, e->m, esz, e->nbuf, e->num_tiles, 64,
+                                  o.chunk_edges, o.tile_degree_max);
     double edges_bytes = 0.9 * ((double)prop.totalGlobalMem - 32.0 * e->n);
-    budget = (uint64_t)(F + std::max(0.0, edges_bytes)) ;
+    budget = (uint64_t)(L0.total + std::max(0.0, edges_bytes));
   }
-  uint64_t cap_full = std::max<uint64_t>(e->m, 1);
-  const size_t slack = 64 * 1024 + 8 * 256;
-  if (budget < F + slack + 64 * per_edge) {
+  const size_t arena = (size_t)std::min<uint64_t>(budget, need);
+  for (int fam = 0; fam < 2; ++fam)
+    e->cap_fam[fam] = fit_cap(fam, o, e->n, e->m, esz, e->nbuf, e->num_tiles, arena);
+  if (e->cap_fam[FAM_INT] == 0) {
+    const Layout L0 = make_layout(FAM_INT, e->n, e->m, esz, e->nbuf, e->num_tiles, 64,
+                                  o.chunk_edges, o.tile_degree_max);
     delete e;
-    return fail(SGW_EBUDGET, "budget %llu B < vertex state %zu B + minimum edge buffers",
-                (unsigned long long)budget, F);
-  }
-  uint64_t cap = (uint64_t)((double)(budget - F - slack) / per_edge);
-  cap = std::min<uint64_t>(cap, cap_full);
-  cap = std::min<uint64_t>(cap, 4294967294ull);  // max_partition_size <= DIST_INFINITY
-  Layout L = make_layout(e->n, e->m, esz, e->nbuf, e->num_tiles, cap, o.chunk_edges, o.tile_degree_max);
-  while (L.total > budget && cap > 64) {
-    cap = cap - std::max<uint64_t>(cap / 64, 64);
-    L = make_layout(e->n, e->m, esz, e->nbuf, e->num_tiles, cap, o.chunk_edges, o.tile_degree_max);
-  }
-  if (L.total > budget) {
-    delete e;
-    return fail(SGW_EBUDGET, "budget %llu B too small (needs %zu B)", (unsigned long long)budget, L.total);
+    return fail(SGW_EBUDGET, "budget %llu B < vertex state and minimum edge buffers (%zu B)",
+                (unsigned long long)budget, L0.total);
   }
   e->budget = budget;
-  cudaError_t ce = cudaMalloc(&e->d_arena, L.total);
+  cudaError_t ce = cudaMalloc(&e->d_arena, arena);
   if (ce != cudaSuccess) {
     delete e;
-    return fail(SGW_ECUDA, "cudaMalloc(%zu): %s", L.total, cudaGetErrorString(ce));
+    return fail(SGW_ECUDA, "cudaMalloc(%zu): %s", arena, cudaGetErrorString(ce));
   }
-  e->arena_bytes = L.total;
-  carve(e, L);
+  e->arena_bytes = arena;
+  carve(e, FAM_INT, e->cap_fam[FAM_INT]);
+  uint32_t parts_host = 0;
+  for (int fam = 0; fam < 2; ++fam)
+    if (e->cap_fam[fam])
+      parts_host = std::max(parts_host, make_layout(fam, e->n, e->m, esz, e->nbuf, e->num_tiles,
+                                                    e->cap_fam[fam], o.chunk_edges, o.tile_degree_max).max_parts);
 
   int st = SGW_OK;
   auto cleanup = [&](int s) { sgw_engine_destroy(e); return s; };
@@ -712,7 +803,7 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   if (cudaEventCreate(&e->ev_t0) != cudaSuccess || cudaEventCreate(&e->ev_t1) != cudaSuccess)
     return cleanup(fail(SGW_ECUDA, "event creation"));
   if (cudaMallocHost(&e->h_ctl, sizeof(Ctl)) != cudaSuccess ||
-      cudaMallocHost(&e->h_parts, sizeof(Part) * (size_t)e->max_parts) != cudaSuccess)
+      cudaMallocHost(&e->h_parts, sizeof(Part) * (size_t)parts_host) != cudaSuccess)
     return cleanup(fail(SGW_ECUDA, "pinned control block"));
   memset(e->h_ctl, 0, sizeof(Ctl));
   ce = cudaMemcpyAsync(e->d_off, g->node_pointer, 4ull * (e->n + 1), cudaMemcpyHostToDevice, e->s_comp);
@@ -854,6 +945,15 @@ int sgw_read_values(sgw_engine *e, void *out_values) {
   if (!e || !out_values) return fail(SGW_EINVAL, "null argument");
   if (!e->initialized) return fail(SGW_ESTATE, "engine not initialised");
   CK(cudaSetDevice(e->device));
+  if (e->fam == FAM_PR) {  // ranks are kept in double: cast on the host
+    std::vector<double> tmp(e->n);
+    CK(cudaMemcpyAsync(tmp.data(), e->d_pval, 8ull * e->n, cudaMemcpyDeviceToHost, e->s_comp));
+    CK(cudaStreamSynchronize(e->s_comp));
+    float *o = static_cast<float *>(out_values);
+    for (uint32_t v = 0; v < e->n; ++v) o[v] = (float)tmp[v];
+    e->stats.d2h_bytes += 8ull * e->n;
+    return SGW_OK;
+  }
   CK(cudaMemcpyAsync(out_values, e->d_value, 4ull * e->n, cudaMemcpyDeviceToHost, e->s_comp));
   CK(cudaStreamSynchronize(e->s_comp));
   e->stats.d2h_bytes += 4ull * e->n;
@@ -861,9 +961,14 @@ int sgw_read_values(sgw_engine *e, void *out_values) {
 }
 
 int sgw_read_values_f64(sgw_engine *e, double *out_values) {
-  (void)e;
-  (void)out_values;
-  return fail(SGW_EINVAL, "PageRank is not available in this build");
+  clear_error();
+  if (!e || !out_values) return fail(SGW_EINVAL, "null argument");
+  if (!e->initialized || e->fam != FAM_PR) return fail(SGW_ESTATE, "no PageRank state");
+  CK(cudaSetDevice(e->device));
+  CK(cudaMemcpyAsync(out_values, e->d_pval, 8ull * e->n, cudaMemcpyDeviceToHost, e->s_comp));
+  CK(cudaStreamSynchronize(e->s_comp));
+  e->stats.d2h_bytes += 8ull * e->n;
+  return SGW_OK;
 }
 
 int sgw_read_active(sgw_engine *e, uint32_t *nodes, uint32_t *ptr, uint32_t capacity, uint32_t *count) {
@@ -904,18 +1009,27 @@ int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values, sgw_run_st
   }
   CK(cudaEventRecord(e->ev_t1, e->s_comp));
   e->stats.global_iterations = gitr;
-  // Graph500 m_reached
-  const uint32_t src = p->algo == SGW_CC ? 0xffffffffu : p->source;
-  k_reached<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->algo, src, e->d_value, e->d_off, e->d_ctl);
-  CK(cudaGetLastError());
+  // Graph500 m_reached (PR: every edge)
+  const bool pr = p->algo == SGW_PR;
+  if (!pr) {
+    const uint32_t src = p->algo == SGW_CC ? 0xffffffffu : p->source;
+    k_reached<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->algo, src, e->d_value, e->d_off, e->d_ctl);
+    CK(cudaGetLastError());
+  }
   if (out_values) {
-    CK(cudaMemcpyAsync(out_values, e->d_value, 4ull * e->n, cudaMemcpyDeviceToHost, e->s_comp));
+    if (pr) {  // the queue is free once the loop is over: cast the ranks into it
+      k_pr_to_f32<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, e->d_pval, (float *)e->d_queue);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(out_values, e->d_queue, 4ull * e->n, cudaMemcpyDeviceToHost, e->s_comp));
+    } else {
+      CK(cudaMemcpyAsync(out_values, e->d_value, 4ull * e->n, cudaMemcpyDeviceToHost, e->s_comp));
+    }
     e->stats.d2h_bytes += 4ull * e->n;
   }
   CK(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
   CK(cudaStreamSynchronize(e->s_comp));
   TRY(check_ctl_error(e));
-  e->stats.reached_edges = e->h_ctl->reached_edges;
+  e->stats.reached_edges = pr ? e->m : e->h_ctl->reached_edges;
   e->stats.relaxed_edges = e->h_ctl->relaxed_edges;
   e->stats.relaxed_sources = e->h_ctl->relaxed_sources;
   float ms = 0;
@@ -1005,7 +1119,9 @@ extern "C" int sgw_generate_noalloc(uint8_t *d_label1, uint8_t *d_label2,
   a.epoch = epoch;
   a.num_tiles = (n + kGenTile - 1) / kGenTile;
   a.consume = consume ? 1 : 0;
-  k_generate<<<a.num_tiles, kGenThreads, 0, s>>>(a);
+  a.delta = a.pval = a.qpush = nullptr;
+  a.acc = a.damping = 0.0;
+  k_generate<false><<<a.num_tiles, kGenThreads, 0, s>>>(a);
   CK(cudaGetLastError());
   Ctl h;
   CK(cudaMemcpyAsync(&h, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));

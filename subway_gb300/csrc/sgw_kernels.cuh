@@ -41,6 +41,7 @@ struct Ctl {
   unsigned long long reached_edges;
   unsigned long long relaxed_edges;
   unsigned long long relaxed_sources;
+  double hub_push;           // single-vertex PR partition: its push value
 };
 
 struct Part {                // one partition of the active queue
@@ -151,6 +152,12 @@ struct GenArgs {
   uint32_t epoch;
   uint32_t num_tiles;
   int consume;               // sync: labels of queued vertices are cleared
+  // PageRank form (activeness delta > acc instead of labels)
+  double *delta;             // pending residual per vertex
+  double *pval;              // accumulated rank per vertex
+  double *qpush;             // per queued vertex: damping * delta / outdeg
+  double acc;
+  double damping;
 };
 
 // One CTA per 4096-vertex tile.  Each warp owns 512 consecutive vertices,
@@ -158,6 +165,13 @@ struct GenArgs {
 // activeness, and only active lanes read their node pointers to get degrees.
 // Active vertices of degree 0 have nothing to relax: their labels are
 // cleared here and they are not queued.
+//
+// PR form (prePrefix PR overload, shared/subgraph_generator.cu:24-41):
+// active = delta > acc.  An active vertex moves its delta into its rank here
+// (value += delta, delta = 0, the first half of pr_kernel,
+// shared/gpu_kernels.cu:234-250) and its queue entry carries the push
+// damping * delta / outdeg, so every round is a bulk-synchronous snapshot.
+template <bool PR>
 __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
   __shared__ uint32_t s_tile;
   __shared__ unsigned long long s_warp[kGenThreads / 32];
@@ -174,13 +188,26 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
 
   uint32_t deg[kGenRounds];
   uint32_t keepmask[kGenRounds];
+  double push[PR ? kGenRounds : 1];
   uint32_t wcount = 0, wedges = 0, seen = 0;
 #pragma unroll
   for (int r = 0; r < kGenRounds; ++r) {
     const uint32_t v = wbase + r * 32 + lane;
     bool act = false;
     uint32_t d = 0;
-    if (v < a.n) {
+    if (PR) {
+      push[PR ? r : 0] = 0.0;
+      if (v < a.n) {
+        const double res = a.delta[v];
+        act = res > a.acc;
+        if (act) {
+          d = __ldg(&a.off[v + 1]) - __ldg(&a.off[v]);
+          a.pval[v] += res;
+          a.delta[v] = 0.0;
+          if (d) push[PR ? r : 0] = a.damping * res / (double)d;
+        }
+      }
+    } else if (v < a.n) {
       act = (a.l1[v] | a.l2[v]) != 0;
       if (act) {
         d = __ldg(&a.off[v + 1]) - __ldg(&a.off[v]);
@@ -229,6 +256,7 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
       const uint32_t pos = (uint32_t)(run >> 32) + __popc(keepmask[r] & lt);
       a.queue[pos] = wbase + r * 32 + lane;
       a.ptr[pos] = (uint32_t)(run & 0xffffffffull) + (incl - deg[r]);
+      if (PR) a.qpush[pos] = push[PR ? r : 0];
     }
     run += ((unsigned long long)__popc(keepmask[r]) << 32) | tot;
   }
@@ -684,6 +712,204 @@ __global__ void k_reached(uint32_t n, int algo, uint32_t source, const uint32_t 
   }
   acc = __reduce_add_sync(0xffffffffu, (uint32_t)acc) ; // per-warp (degree sums fit u32 per warp)
   if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&ctl->reached_edges, acc);
+}
+
+// ---- PageRank (pr_kernel / pr_async, shared/gpu_kernels.cu:211-254, :459-502) --
+// Ranks and residuals are kept in double precision on the device; the
+// reference's float results are the final cast.
+struct PrItem {              // a chunk of one high-degree source's pushes
+  uint32_t boff;
+  uint32_t count;
+  double push;
+};
+
+struct PrArgs {
+  const uint32_t *queue;
+  const uint32_t *ptr;
+  const uint32_t *buf;       // device edge buffer (W words per edge)
+  double *pval;
+  double *delta;
+  const double *qpush;       // pushes snapshotted by the generate step
+  Ctl *ctl;
+  PrItem *wl;
+  uint32_t wl_cap;
+  uint32_t from, size, edge_from;
+  uint32_t iter;
+  uint32_t tile_degree_max;
+  uint32_t chunk_edges;
+  double acc;
+  double damping;
+};
+
+__device__ __forceinline__ double ld_relaxed_f64(const double *p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Same tiling as k_relax_tile.  Inner iteration 1 pushes the snapshot taken
+// by the generate step (every queued source is active); async iterations > 1
+// re-activate partition sources whose residual grew above acc
+// (value += delta; delta -= delta, atomically against concurrent pushes).
+template <bool ASYNC, int W>
+__global__ void __launch_bounds__(kRelaxThreads) k_pr_tile(PrArgs a) {
+  __shared__ uint32_t s_scan[kRelaxThreads + 1];
+  __shared__ uint32_t s_boff[kRelaxThreads];
+  __shared__ double s_push[kRelaxThreads];
+  __shared__ uint32_t s_hub[kRelaxThreads];
+  __shared__ uint32_t s_wsum[kRelaxThreads / 32];
+  __shared__ uint32_t s_nhub, s_wbase;
+  __shared__ int s_skip;
+  const int tid = threadIdx.x;
+  const uint32_t slot = a.iter & 3u;
+  if (tid == 0) {
+    int skip = 0;
+    if (ASYNC && a.iter > 1 && ld_acquire_u32(&a.ctl->upd[(a.iter - 1) & 3u]) == 0) skip = 1;
+    s_skip = skip;
+    if (blockIdx.x == 0) {
+      a.ctl->upd[(a.iter + 1) & 3u] = 0;
+      a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
+      if (!skip) atomicAdd(&a.ctl->iters_run, 1u);
+    }
+  }
+  __syncthreads();
+  if (s_skip) return;
+  bool any_push = false;
+  const uint32_t ntiles = (a.size + kRelaxThreads - 1) / kRelaxThreads;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    if (tid == 0) s_nhub = 0;
+    __syncthreads();
+    const uint32_t i = a.from + t * kRelaxThreads + tid;
+    uint32_t d = 0, boff = 0;
+    double push = 0.0;
+    if (i < a.from + a.size) {
+      const uint32_t p0 = a.ptr[i];
+      const uint32_t deg = a.ptr[i + 1] - p0;
+      bool act;
+      if (!ASYNC || a.iter == 1) {
+        push = a.qpush[i];
+        act = true;
+      } else {
+        const uint32_t u = a.queue[i];
+        const double res = ld_relaxed_f64(&a.delta[u]);
+        act = res > a.acc;
+        if (act) {
+          a.pval[u] += res;
+          atomicAdd(&a.delta[u], -res);
+          push = a.damping * res / (double)deg;
+        }
+      }
+      if (act) {
+        any_push = true;
+        d = deg;
+        boff = p0 - a.edge_from;
+        if (d > a.tile_degree_max) {
+          s_hub[atomicAdd(&s_nhub, 1u)] = tid;
+          atomicAdd(&a.ctl->relaxed_edges, (unsigned long long)d);
+        }
+      }
+    }
+    s_boff[tid] = boff;
+    s_push[tid] = push;
+    {
+      const int nsrc = __syncthreads_count(d > 0);
+      if (tid == 0 && nsrc) atomicAdd(&a.ctl->relaxed_sources, (unsigned long long)nsrc);
+    }
+    const uint32_t nhub = s_nhub;
+    for (uint32_t h = 0; h < nhub; ++h) {
+      const uint32_t ht = s_hub[h];
+      if (tid == ht) {
+        s_wbase = atomicAdd(&a.ctl->wl_count[slot], (d + a.chunk_edges - 1) / a.chunk_edges);
+        s_scan[kRelaxThreads] = d;
+      }
+      __syncthreads();
+      const uint32_t hd = s_scan[kRelaxThreads];
+      const uint32_t nch = (hd + a.chunk_edges - 1) / a.chunk_edges;
+      const uint32_t wb = s_wbase;
+      for (uint32_t c = tid; c < nch; c += blockDim.x) {
+        if (wb + c < a.wl_cap) {
+          PrItem it;
+          it.boff = s_boff[ht] + c * a.chunk_edges;
+          it.count = min(a.chunk_edges, hd - c * a.chunk_edges);
+          it.push = s_push[ht];
+          a.wl[wb + c] = it;
+        } else {
+          atomicExch(&a.ctl->error, 3u);
+        }
+      }
+      __syncthreads();
+    }
+    if (d > a.tile_degree_max) d = 0;
+    {
+      const int lane = tid & 31, warp = tid >> 5;
+      const uint32_t incl = warp_incl_scan(d, lane);
+      if (lane == 31) s_wsum[warp] = incl;
+      __syncthreads();
+      if (tid == 0) {
+        uint32_t acc = 0;
+        for (int w = 0; w < kRelaxThreads / 32; ++w) { uint32_t x = s_wsum[w]; s_wsum[w] = acc; acc += x; }
+        s_scan[kRelaxThreads] = acc;
+      }
+      __syncthreads();
+      s_scan[tid] = s_wsum[warp] + incl - d;
+      __syncthreads();
+    }
+    const uint32_t total = s_scan[kRelaxThreads];
+    if (tid == 0 && total) atomicAdd(&a.ctl->relaxed_edges, (unsigned long long)total);
+    for (uint32_t j = tid; j < total; j += blockDim.x) {
+      uint32_t lo = 0, hi = kRelaxThreads;
+      while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (s_scan[mid] <= j) lo = mid + 1; else hi = mid;
+      }
+      const uint32_t k = lo - 1;
+      const uint32_t e = s_boff[k] + (j - s_scan[k]);
+      const uint32_t dst = a.buf[(size_t)e * W];
+      atomicAdd(&a.delta[dst], s_push[k]);
+    }
+    __syncthreads();
+  }
+  if (__syncthreads_or(any_push) && tid == 0) atomicAdd(&a.ctl->upd[slot], 1u);
+}
+
+template <bool ASYNC, int W>
+__global__ void __launch_bounds__(kRelaxThreads) k_pr_chunks(PrArgs a) {
+  const uint32_t slot = a.iter & 3u;
+  if (ASYNC && a.iter > 1 && ld_acquire_u32(&a.ctl->upd[(a.iter - 1) & 3u]) == 0) return;
+  const uint32_t items = min(ld_acquire_u32(&a.ctl->wl_count[slot]), a.wl_cap);
+  const int lane = threadIdx.x & 31;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t it = gw; it < items; it += nw) {
+    const PrItem wi = a.wl[it];
+    for (uint32_t j = lane; j < wi.count; j += 32)
+      atomicAdd(&a.delta[a.buf[(size_t)(wi.boff + j) * W]], wi.push);
+  }
+}
+
+// Single-vertex PR partition: the generate snapshot of its push.
+__global__ void k_pr_hub_claim(uint32_t from, const double *qpush, Ctl *ctl) {
+  ctl->hub_push = qpush[from];
+}
+
+template <int W>
+__global__ void k_pr_flat(const uint32_t *buf, uint32_t count, double *delta, const Ctl *ctl) {
+  const double push = ctl->hub_push;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
+    atomicAdd(&delta[buf[(size_t)j * W]], push);
+}
+
+// delta = init, value = 0 (subway/pr-sync.cu:36-40).
+__global__ void k_pr_init(uint32_t n, double init, double *pval, double *delta) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    pval[v] = 0.0;
+    delta[v] = init;
+  }
+}
+
+__global__ void k_pr_to_f32(uint32_t n, const double *pval, float *out) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    out[v] = (float)pval[v];
 }
 
 }  // namespace sgw

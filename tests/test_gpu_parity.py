@@ -137,10 +137,91 @@ def test_hub_larger_than_budget(gpu, orc):
     w = (1 + (src * 7 + dst * 13) % 50).astype(np.uint32)
     edges = np.stack([dst.astype(np.uint32), w], 1)
     g = gpu.Graph.from_csr(npt, edges, True)
-    eng = gpu.Engine(g, budget_bytes=18 * n + 72 * 1024 + 500 * 16)
+    eng = gpu.Engine(g, budget_bytes=18 * n + 12 * 1024 + 1000 * 16)
     assert eng.max_partition_size() < 2500
     for algo in ("bfs", "sssp", "sswp", "cc"):
         for mode in MODES:
             vals, _ = eng.run(algo, mode, 0)
             ref = _oracle(orc, g, algo, 0)
             assert np.array_equal(vals, ref), (algo, mode)
+
+
+# ---- PageRank ------------------------------------------------------------------
+PR_INIT, PR_ACC, PR_DAMP = (float(np.float32(x)) for x in (0.15, 0.01, 0.85))
+
+
+def _pr_engine_values(gpu, eng):
+    import ctypes as C
+    out = np.empty(eng.graph.n, np.float64)
+    gpu.check(gpu.lib().sgw_read_values_f64(eng.h, out.ctypes.data), "sgw_read_values_f64")
+    return out
+
+
+@pytest.mark.parametrize("budget_edges", [None, 300, 5000])
+def test_pagerank_sync_matches_bsp_oracle(gpu, orc, g12u, budget_edges):
+    """Sync PR is the bulk-synchronous delta schedule: FP64 ranks agree with
+    the FP64 oracle to 1e-9 (max-abs); the FP32 output is their cast."""
+    g = g12u
+    kw = {} if budget_edges is None else {"budget_bytes": 36 * g.n + 96 * 1024 + budget_edges * 8}
+    eng = gpu.Engine(g, **kw)
+    vals, st = eng.run("pr", "sync")
+    ref, rounds = orc.pagerank(g.node_pointer, g.edges, init=PR_INIT, acc=PR_ACC, damping=PR_DAMP)
+    f64 = _pr_engine_values(gpu, eng)
+    assert np.max(np.abs(f64 - ref)) <= 1e-9
+    assert np.array_equal(vals, ref.astype(np.float32)) or np.max(np.abs(vals - ref) / np.maximum(ref, 1e-30)) < 2.5e-7
+    assert st["global_iterations"] == rounds
+
+
+@pytest.mark.parametrize("budget_edges", [None, 2000])
+def test_pagerank_async_within_residual_bound(gpu, orc, g12u, budget_edges):
+    """Async PR stops with every residual <= acc, so each rank is within
+    (acc / init) x its exact value of the fixpoint."""
+    g = g12u
+    kw = {} if budget_edges is None else {"budget_bytes": 36 * g.n + 96 * 1024 + budget_edges * 8}
+    eng = gpu.Engine(g, **kw)
+    eng.run("pr", "async")
+    f64 = _pr_engine_values(gpu, eng)
+    exact, _ = orc.pagerank(g.node_pointer, g.edges, init=PR_INIT, acc=1e-14, damping=PR_DAMP)
+    assert np.all(np.abs(f64 - exact) <= (PR_ACC / PR_INIT) * exact + 1e-9)
+    assert np.all(f64 <= exact + 1e-9), "delta-PR only adds mass: ranks approach the fixpoint from below"
+
+
+def test_pagerank_tight_tolerance(gpu, orc):
+    """With acc = 1e-6 the FP64 ranks are within 1e-6 (max-abs) of the FP64
+    oracle's exact fixpoint on an ER graph."""
+    g = gpu.Graph.er(3000, 30000, seed=4)
+    eng = gpu.Engine(g)
+    acc = float(np.float32(1e-6))
+    eng.run("pr", "sync", pr_acc=acc)
+    f64 = _pr_engine_values(gpu, eng)
+    ref, _ = orc.pagerank(g.node_pointer, g.edges, init=PR_INIT, acc=acc, damping=PR_DAMP)
+    assert np.max(np.abs(f64 - ref)) <= 1e-9
+    exact, _ = orc.pagerank(g.node_pointer, g.edges, init=PR_INIT, acc=1e-15, damping=PR_DAMP)
+    assert np.max(np.abs(f64 - exact)) <= 1e-4
+
+
+def test_engine_matches_reference_golden(gpu):
+    """The engine against the reference build's own outputs (tests/golden)."""
+    from pathlib import Path
+    d = np.load(Path(__file__).resolve().parent / "golden" / "ref_rmat13.npz")
+    scale, ef, seed, wmax, _ = (int(x) for x in d["params"])
+    gu = gpu.Graph.rmat(scale, ef, seed=seed)
+    gw = gpu.Graph.rmat(scale, ef, seed=seed, weighted=True, wmax=wmax)
+    engines = {False: gpu.Engine(gu, budget_bytes=36 * gu.n + 96 * 1024 + 20000 * 8),
+               True: gpu.Engine(gw, budget_bytes=36 * gw.n + 96 * 1024 + 20000 * 16)}
+    for k in d.keys():
+        if not k.startswith("fixed/"):
+            continue
+        _, app, *s = k.split("/")
+        algo, mode = app.split("-")
+        eng = engines[algo in ("sssp", "sswp")]
+        src = int(s[0][1:]) if s else 0
+        vals, _ = eng.run(algo, mode, src)
+        if algo == "pr":
+            ref = d[k].astype(np.float64)
+            if mode == "sync":
+                assert np.max(np.abs(vals - ref) / ref) < 1e-5, k
+            else:
+                assert np.max(np.abs(vals - ref) / ref) < PR_ACC / PR_INIT, k
+        else:
+            assert np.array_equal(vals, d[k]), k
