@@ -59,6 +59,11 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=24)
     ap.add_argument("--cpu-sample", type=int, default=8, help="sources timed for the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-pack", action="store_true", help="move the reference's 8-byte records")
+    ap.add_argument("--gather-ctas", type=int, default=0)
+    ap.add_argument("--tile-degree-max", type=int, default=0)
+    ap.add_argument("--chunk-edges", type=int, default=0)
+    ap.add_argument("--inner-batch", type=int, default=0)
     return ap.parse_args()
 
 
@@ -193,7 +198,9 @@ def run_ours(a, dist):
     g = N.Graph.rmat(a.scale, a.edge_factor, seed=a.seed, weighted=weighted, wmax=64)
     sources = g.pick_sources(a.sources, seed=a.seed)
     t_gen = time.time() - t0
-    eng = N.Engine(g, budget_bytes=int(a.budget), device=dev, flags=N.OPT_PROFILE)
+    flags = N.OPT_PROFILE | (N.OPT_NO_PACK if a.no_pack else 0)
+    eng = N.Engine(g, budget_bytes=int(a.budget), device=dev, flags=flags, gather_ctas=a.gather_ctas,
+                   tile_degree_max=a.tile_degree_max, chunk_edges=a.chunk_edges, inner_batch=a.inner_batch)
     h2d_peak, d2h_peak = probe_link(N, dev)
     import numpy as np
     out = np.empty(g.n, np.uint32)  # host result buffer
@@ -258,7 +265,8 @@ def run_ours(a, dist):
         "metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": dist.world, "steps": K,
         "warmup": a.warmup, "ms_per_step": round(dev_ms_max / K, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": workload_config(a, {"policy": "plain"}),
+        "config": workload_config(a, {"policy": "plain",
+                                      "transfer_record_bytes": 4 if (weighted and not a.no_pack) or not weighted else 8}),
         "e2e": {"value": round(e2e, 4), "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(wall_ms_max / K, 4)},
         "h2d_bytes_per_run": int(h2d),

@@ -91,6 +91,11 @@ void sgw_graph_free(sgw_graph *g);
 /* ---- engine --------------------------------------------------------------- */
 #define SGW_OPT_PROFILE   0x1u  /* time every kernel class with CUDA events   */
 #define SGW_OPT_NO_OVERLAP 0x2u /* one edge buffer, no copy/compute overlap   */
+/* Weighted graphs are moved as one 32-bit word per edge, (w8 << b) | end with
+ * b = bits of the largest vertex id, whenever every weight fits in 32 - b
+ * bits (a packed copy of the edges is built in host memory at engine
+ * creation).  This flag keeps the reference's 8-byte records instead. */
+#define SGW_OPT_NO_PACK    0x4u
 
 typedef struct sgw_engine_opts {
   /* Device-memory budget in bytes for everything the engine allocates.

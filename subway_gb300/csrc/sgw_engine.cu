@@ -75,8 +75,13 @@ struct sgw_engine {
   // host side
   Ctl *h_ctl = nullptr;
   Part *h_parts = nullptr;
-  const uint32_t *d_host_edges = nullptr;
+  const uint32_t *d_host_edges = nullptr;  // device view of the transfer records
+  const void *h_src = nullptr;             // host view of the transfer records
   bool registered = false;
+  uint32_t *h_packed = nullptr;            // packed transfer copy (weighted graphs)
+  size_t packed_bytes = 0;
+  bool packed_registered = false;
+  uint32_t pbits = 0;                      // packed: bits of the destination id
   cudaStream_t s_comp = nullptr, s_copy = nullptr;
   cudaEvent_t ev_ready[2] = {}, ev_free[2] = {};
   cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
@@ -389,6 +394,7 @@ int launch_relax_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, u
   a.iter = iter;
   a.tile_degree_max = e->opts.tile_degree_max;
   a.chunk_edges = e->opts.chunk_edges;
+  a.pbits = e->pbits;
   const uint32_t g1 = grid_for(e, q.size, kRelaxThreads);
   k_relax_tile<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
   CK(cudaGetLastError());
@@ -431,6 +437,7 @@ int launch_pr_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter) {
   a.iter = iter;
   a.tile_degree_max = e->opts.tile_degree_max;
   a.chunk_edges = e->opts.chunk_edges;
+  a.pbits = e->pbits;
   a.acc = (double)e->params.pr_acc;
   a.damping = (double)e->params.pr_damping;
   k_pr_tile<ASYNC, W><<<grid_for(e, q.size, kRelaxThreads), kRelaxThreads, 0, e->s_comp>>>(a);
@@ -460,8 +467,8 @@ int launch_relax(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, bool a
 
 template <int ALGO, int W>
 int launch_flat_w(sgw_engine *e, uint32_t b, uint32_t count) {
-  k_relax_flat<ALGO, W><<<grid_for(e, count, 256), 256, 0, e->s_comp>>>(e->d_buf[b], count, e->d_value,
-                                                                       e->d_l2, e->d_ctl);
+  k_relax_flat<ALGO, W><<<grid_for(e, count, 256), 256, 0, e->s_comp>>>(e->d_buf[b], count, e->pbits,
+                                                                       e->d_value, e->d_l2, e->d_ctl);
   CK(cudaGetLastError());
   return SGW_OK;
 }
@@ -487,7 +494,7 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
     const uint32_t cnt = (uint32_t)std::min<uint64_t>(e->cap, deg - s);
     size_t slot = 0;
     TRY(prof_begin(e, K_GATHER, e->s_comp, &slot));
-    CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->g->edges + (hoff + s) * esz, cnt * esz,
+    CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->h_src + (hoff + s) * esz, cnt * esz,
                        cudaMemcpyHostToDevice, e->s_comp));
     TRY(prof_end(e, e->s_comp, slot));
     e->stats.h2d_bytes += cnt * esz;
@@ -495,8 +502,8 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
     int st = SGW_OK;
     switch (e->params.algo) {
       case SGW_PR:
-        if (e->W == 1) k_pr_flat<1><<<grid_for(e, cnt, 256), 256, 0, e->s_comp>>>(e->d_buf[b], cnt, e->d_delta, e->d_ctl);
-        else k_pr_flat<2><<<grid_for(e, cnt, 256), 256, 0, e->s_comp>>>(e->d_buf[b], cnt, e->d_delta, e->d_ctl);
+        if (e->W == 1) k_pr_flat<1><<<grid_for(e, cnt, 256), 256, 0, e->s_comp>>>(e->d_buf[b], cnt, e->pbits, e->d_delta, e->d_ctl);
+        else k_pr_flat<2><<<grid_for(e, cnt, 256), 256, 0, e->s_comp>>>(e->d_buf[b], cnt, e->pbits, e->d_delta, e->d_ctl);
         if (cudaGetLastError() != cudaSuccess) st = fail(SGW_ECUDA, "k_pr_flat launch");
         break;
       case SGW_BFS: st = launch_flat<SGW_BFS>(e, b, cnt); break;
@@ -731,6 +738,13 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   e->n = g->n;
   e->m = g->m;
   e->W = g->weighted ? 2 : 1;
+  e->h_src = g->edges;
+  // weighted records travel as one packed word when (w << bits(n)) | dst fits
+  if (g->weighted && !(o.flags & SGW_OPT_NO_PACK) &&
+      pack_weighted(g, &e->h_packed, &e->packed_bytes, &e->pbits)) {
+    e->W = 1;
+    e->h_src = e->h_packed;
+  }
   e->nbuf = (o.flags & SGW_OPT_NO_OVERLAP) ? 1 : 2;
   e->num_tiles = (uint32_t)((g->n + kGenTile - 1) / kGenTile);
   cudaDeviceProp prop;
@@ -781,7 +795,15 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   auto cleanup = [&](int s) { sgw_engine_destroy(e); return s; };
   // host edges readable by device kernels (mapped pinned memory)
   const size_t ebytes = std::max<size_t>((size_t)e->m * esz, 4);
-  if (g->m > 0) {
+  if (g->m > 0 && e->h_packed) {
+    ce = cudaHostRegister(e->h_packed, e->packed_bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
+    if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostRegister: %s", cudaGetErrorString(ce))); }
+    e->packed_registered = true;
+    void *dp = nullptr;
+    ce = cudaHostGetDevicePointer(&dp, e->h_packed, 0);
+    if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce))); }
+    e->d_host_edges = (const uint32_t *)dp;
+  } else if (g->m > 0) {
     size_t reg_bytes = g->owns ? g->edges_bytes_alloc : ebytes;
     ce = cudaHostRegister(g->edges, reg_bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
     if (ce == cudaSuccess) e->registered = true;
@@ -833,6 +855,8 @@ int sgw_engine_destroy(sgw_engine *e) {
   if (e->h_ctl) cudaFreeHost(e->h_ctl);
   if (e->h_parts) cudaFreeHost(e->h_parts);
   if (e->registered) cudaHostUnregister(e->g->edges);
+  if (e->packed_registered) cudaHostUnregister(e->h_packed);
+  if (e->h_packed) host_free(e->h_packed);
   if (e->d_arena) cudaFree(e->d_arena);
   cudaGetLastError();
   delete e;

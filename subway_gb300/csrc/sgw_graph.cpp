@@ -69,6 +69,26 @@ int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out) {
   return SGW_OK;
 }
 
+bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint32_t *nbits) {
+  *out = nullptr;
+  if (!g->weighted || g->m == 0) return false;
+  uint32_t nb = 1;
+  while (nb < 32 && (uint64_t(1) << nb) < g->n) ++nb;
+  if (nb >= 31) return false;
+  const uint32_t *ed = (const uint32_t *)g->edges;
+  uint32_t wmax = 0;
+#pragma omp parallel for reduction(max : wmax)
+  for (int64_t i = 0; i < (int64_t)g->m; ++i) wmax = std::max(wmax, ed[2 * size_t(i) + 1]);
+  if ((uint64_t)wmax >= (uint64_t(1) << (32 - nb))) return false;
+  uint32_t *p = (uint32_t *)host_alloc(sizeof(uint32_t) * size_t(g->m), alloc_bytes);
+  if (!p) return false;
+#pragma omp parallel for
+  for (int64_t i = 0; i < (int64_t)g->m; ++i) p[i] = (ed[2 * size_t(i) + 1] << nb) | ed[2 * size_t(i)];
+  *out = p;
+  *nbits = nb;
+  return true;
+}
+
 // ---- SplitMix64 ------------------------------------------------------------
 static inline uint64_t mix64(uint64_t z) {
   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;

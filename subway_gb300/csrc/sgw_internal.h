@@ -32,6 +32,11 @@ void host_free(void *p);
 // Creates a graph object owning freshly allocated arrays.
 int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out);
 
+// Transfer format for weighted graphs: one u32 per edge, (w << nbits) | dst,
+// with nbits = bits of the largest vertex id.  Returns false, allocating
+// nothing, when some weight does not fit in the remaining 32 - nbits bits.
+bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint32_t *nbits);
+
 // Greedy partition planner shared by the host entry point and the device
 // planner: largest prefix of the queue starting at `from` whose edge count
 // is <= cap, at least one vertex.

@@ -448,6 +448,23 @@ __device__ __forceinline__ bool can_push(uint32_t v) {
   return true;
 }
 
+// Reads edge record e of a device edge buffer: W = 2 words {end, w8};
+// W = 1 either an unweighted {end} (pbits = 0) or the packed transfer form
+// (w8 << pbits) | end.
+template <int W>
+__device__ __forceinline__ void load_edge(const uint32_t *buf, uint32_t e, uint32_t pbits,
+                                          uint32_t &dst, uint32_t &w) {
+  if (W == 1) {
+    const uint32_t r = buf[e];
+    if (pbits) { dst = r & ((1u << pbits) - 1u); w = r >> pbits; }
+    else { dst = r; w = 0; }
+  } else {
+    const uint2 ed = reinterpret_cast<const uint2 *>(buf)[e];
+    dst = ed.x;
+    w = ed.y;
+  }
+}
+
 struct RelaxArgs {
   const uint32_t *queue;
   const uint32_t *ptr;
@@ -462,6 +479,7 @@ struct RelaxArgs {
   uint32_t iter;             // inner iteration number (1-based)
   uint32_t tile_degree_max;  // sources above this go to the chunk list
   uint32_t chunk_edges;
+  uint32_t pbits;            // packed records: bits of the destination
 };
 
 constexpr int kRelaxThreads = 256;
@@ -583,14 +601,8 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
       }
       const uint32_t k = lo - 1;
       const uint32_t e = s_boff[k] + (j - s_scan[k]);
-      uint32_t dst, w = 0;
-      if (W == 1) {
-        dst = a.buf[e];
-      } else {
-        const uint2 ed = reinterpret_cast<const uint2 *>(a.buf)[e];
-        dst = ed.x;
-        w = ed.y;
-      }
+      uint32_t dst, w;
+      load_edge<W>(a.buf, e, a.pbits, dst, w);
       any_update |= relax_edge<ALGO>(s_val[k], dst, w, a.value, a.nxt);
     }
     __syncthreads();
@@ -611,15 +623,8 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_chunks(RelaxArgs a) {
   for (uint32_t it = gw; it < items; it += nw) {
     const WorkItem wi = a.wl[it];
     for (uint32_t j = lane; j < wi.count; j += 32) {
-      const uint32_t e = wi.boff + j;
-      uint32_t dst, w = 0;
-      if (W == 1) {
-        dst = a.buf[e];
-      } else {
-        const uint2 ed = reinterpret_cast<const uint2 *>(a.buf)[e];
-        dst = ed.x;
-        w = ed.y;
-      }
+      uint32_t dst, w;
+      load_edge<W>(a.buf, wi.boff + j, a.pbits, dst, w);
       any_update |= relax_edge<ALGO>(wi.value, dst, w, a.value, a.nxt);
     }
   }
@@ -642,16 +647,15 @@ __global__ void k_hub_claim(uint32_t u, const uint32_t *value, uint8_t *l1, uint
 }
 
 template <int ALGO, int W>
-__global__ void k_relax_flat(const uint32_t *buf, uint32_t count, uint32_t *value,
+__global__ void k_relax_flat(const uint32_t *buf, uint32_t count, uint32_t pbits, uint32_t *value,
                              uint8_t *nxt, Ctl *ctl) {
   if (!ctl->hub_active) return;
   const uint32_t sval = ctl->hub_value;
   if (!can_push<ALGO>(sval)) return;
   bool any = false;
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
-    uint32_t dst, w = 0;
-    if (W == 1) dst = buf[j];
-    else { const uint2 ed = reinterpret_cast<const uint2 *>(buf)[j]; dst = ed.x; w = ed.y; }
+    uint32_t dst, w;
+    load_edge<W>(buf, j, pbits, dst, w);
     any |= relax_edge<ALGO>(sval, dst, w, value, nxt);
   }
   if (__syncthreads_or(any) && threadIdx.x == 0) atomicAdd(&ctl->upd[1], 1u);
@@ -737,6 +741,7 @@ struct PrArgs {
   uint32_t iter;
   uint32_t tile_degree_max;
   uint32_t chunk_edges;
+  uint32_t pbits;
   double acc;
   double damping;
 };
@@ -863,8 +868,8 @@ __global__ void __launch_bounds__(kRelaxThreads) k_pr_tile(PrArgs a) {
         if (s_scan[mid] <= j) lo = mid + 1; else hi = mid;
       }
       const uint32_t k = lo - 1;
-      const uint32_t e = s_boff[k] + (j - s_scan[k]);
-      const uint32_t dst = a.buf[(size_t)e * W];
+      uint32_t dst, w;
+      load_edge<W>(a.buf, s_boff[k] + (j - s_scan[k]), a.pbits, dst, w);
       atomicAdd(&a.delta[dst], s_push[k]);
     }
     __syncthreads();
@@ -882,8 +887,11 @@ __global__ void __launch_bounds__(kRelaxThreads) k_pr_chunks(PrArgs a) {
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t it = gw; it < items; it += nw) {
     const PrItem wi = a.wl[it];
-    for (uint32_t j = lane; j < wi.count; j += 32)
-      atomicAdd(&a.delta[a.buf[(size_t)(wi.boff + j) * W]], wi.push);
+    for (uint32_t j = lane; j < wi.count; j += 32) {
+      uint32_t dst, w;
+      load_edge<W>(a.buf, wi.boff + j, a.pbits, dst, w);
+      atomicAdd(&a.delta[dst], wi.push);
+    }
   }
 }
 
@@ -893,10 +901,14 @@ __global__ void k_pr_hub_claim(uint32_t from, const double *qpush, Ctl *ctl) {
 }
 
 template <int W>
-__global__ void k_pr_flat(const uint32_t *buf, uint32_t count, double *delta, const Ctl *ctl) {
+__global__ void k_pr_flat(const uint32_t *buf, uint32_t count, uint32_t pbits, double *delta,
+                          const Ctl *ctl) {
   const double push = ctl->hub_push;
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x)
-    atomicAdd(&delta[buf[(size_t)j * W]], push);
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+    uint32_t dst, w;
+    load_edge<W>(buf, j, pbits, dst, w);
+    atomicAdd(&delta[dst], push);
+  }
 }
 
 // delta = init, value = 0 (subway/pr-sync.cu:36-40).

@@ -20,6 +20,7 @@ SYNC, ASYNC = 0, 1
 INF = 4294967294
 OPT_PROFILE = 0x1
 OPT_NO_OVERLAP = 0x2
+OPT_NO_PACK = 0x4
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
 MODES = {"sync": SYNC, "async": ASYNC}
 

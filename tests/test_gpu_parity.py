@@ -225,3 +225,28 @@ def test_engine_matches_reference_golden(gpu):
                 assert np.max(np.abs(vals - ref) / ref) < PR_ACC / PR_INIT, k
         else:
             assert np.array_equal(vals, d[k]), k
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_reference_records_without_packing(gpu, orc, g12w, mode):
+    """SGW_OPT_NO_PACK moves the reference's 8-byte records; same answers."""
+    g = g12w
+    eng = gpu.Engine(g, budget_bytes=18 * g.n + 72 * 1024 + 3000 * 16, flags=gpu.OPT_NO_PACK)
+    src = int(g.pick_sources(1, seed=9)[0])
+    for algo in ALGS:
+        vals, _ = eng.run(algo, mode, src)
+        assert np.array_equal(vals, _oracle(orc, g, algo, src)), (algo, mode)
+
+
+def test_wide_weights_fall_back_to_full_records(gpu, orc):
+    """Weights that do not fit beside the vertex id keep 8-byte records."""
+    g0 = gpu.Graph.rmat(12, 8, seed=13, weighted=True)
+    e = np.array(g0.edges)
+    e[:, 1] = (e[:, 1].astype(np.uint64) * 40503 % (1 << 22) + 1).astype(np.uint32)  # 22-bit weights
+    g = gpu.Graph.from_csr(np.array(g0.node_pointer), e, True)
+    eng = gpu.Engine(g, budget_bytes=18 * g.n + 72 * 1024 + 2000 * 16)
+    for algo in ("sssp", "sswp"):
+        for mode in MODES:
+            vals, st = eng.run(algo, mode, 0)
+            assert np.array_equal(vals, _oracle(orc, g, algo, 0)), (algo, mode)
+    assert st["h2d_bytes"] % 8 == 0
