@@ -96,6 +96,8 @@ void sgw_graph_free(sgw_graph *g);
  * bits (a packed copy of the edges is built in host memory at engine
  * creation).  This flag keeps the reference's 8-byte records instead. */
 #define SGW_OPT_NO_PACK    0x4u
+/* Gather host records one per thread instead of as aligned 16-byte words. */
+#define SGW_OPT_SCALAR_GATHER 0x8u
 
 typedef struct sgw_engine_opts {
   /* Device-memory budget in bytes for everything the engine allocates.

@@ -81,6 +81,7 @@ struct sgw_engine {
   uint32_t *h_packed = nullptr;            // packed transfer copy (weighted graphs)
   size_t packed_bytes = 0;
   bool packed_registered = false;
+  bool vec_gather = false;                 // host records readable as aligned 16-B words
   uint32_t pbits = 0;                      // packed: bits of the destination id
   cudaStream_t s_comp = nullptr, s_copy = nullptr;
   cudaEvent_t ev_ready[2] = {}, ev_free[2] = {};
@@ -358,7 +359,14 @@ int enqueue_gather(sgw_engine *e, uint32_t p, cudaStream_t s) {
   TRY(prof_begin(e, K_GATHER, s, &slot));
   const uint32_t gmax = e->opts.gather_ctas ? e->opts.gather_ctas : 2u * e->num_sms;
   const uint32_t grid = std::min<uint32_t>(grid_for(e, q.edge_count, kGatherTile), gmax);
-  if (e->W == 1)
+  const uint4 *h16 = reinterpret_cast<const uint4 *>(e->d_host_edges);
+  if (e->vec_gather && e->W == 1)
+    k_gather_v<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+                                                  q.from, q.size, q.edge_from, (uint32_t)q.edge_count);
+  else if (e->vec_gather)
+    k_gather_v<2><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+                                                  q.from, q.size, q.edge_from, (uint32_t)q.edge_count);
+  else if (e->W == 1)
     k_gather<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_edges,
                                                 e->d_buf[b], q.from, q.size, q.edge_from,
                                                 (uint32_t)q.edge_count);
@@ -813,6 +821,15 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
     ce = cudaHostGetDevicePointer(&dp, g->edges, 0);
     if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce))); }
     e->d_host_edges = (const uint32_t *)dp;
+  }
+  // 16-byte host reads may run up to 12 bytes past the last record: allowed
+  // when the registered range is page-rounded (the library's allocations) or
+  // the record array is a whole number of 16-byte words.
+  {
+    const size_t rec_bytes = (size_t)e->m * 4 * e->W;
+    const bool rounded = e->h_packed != nullptr || g->owns || (rec_bytes % 16 == 0);
+    e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && e->d_host_edges &&
+                    ((uintptr_t)e->d_host_edges % 16 == 0) && rounded;
   }
   if (cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking) != cudaSuccess)

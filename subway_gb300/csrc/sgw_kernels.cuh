@@ -402,6 +402,126 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(
   }
 }
 
+// Same tiling as k_gather, but host memory is read as aligned 16-byte words:
+// each source's clipped host range is covered by ceil-aligned chunks of
+// R = 4 / W records, the CTA scans the chunk counts of its tile's sources, and
+// every thread loads whole chunks (4 in flight) and scatters the records that
+// belong to the source into the device buffer.  Needs a 16-byte aligned host
+// array (the engine's own allocations are 64 KiB aligned).
+template <int W>
+__global__ void __launch_bounds__(kGatherThreads) k_gather_v(
+    const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
+    const uint32_t *__restrict__ off, const uint4 *__restrict__ host16,
+    uint32_t *__restrict__ buf, uint32_t from, uint32_t size, uint32_t edge_from,
+    uint32_t edge_count) {
+  constexpr uint32_t R = 4 / W;  // records per 16-byte chunk
+  __shared__ uint32_t s_bpos[kGatherTile + 1];
+  __shared__ uint32_t s_hlo[kGatherTile + 1];
+  __shared__ uint32_t s_len[kGatherTile + 1];
+  __shared__ uint32_t s_cs[kGatherTile + 1];
+  __shared__ uint32_t s_part[kGatherThreads + 1];
+  __shared__ uint32_t s_first, s_nsrc;
+  const uint32_t ntiles = (edge_count + kGatherTile - 1) / kGatherTile;
+  const int tid = threadIdx.x;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t j0 = t * kGatherTile;
+    const uint32_t j1 = min(edge_count, j0 + kGatherTile);
+    if (tid == 0) {
+      uint32_t lo = from, hi = from + size;
+      while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (ptr[mid] - edge_from <= j0) lo = mid; else hi = mid;
+      }
+      const uint32_t first = lo;
+      lo = first;
+      hi = from + size;
+      while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (ptr[mid] - edge_from <= j1 - 1) lo = mid; else hi = mid;
+      }
+      s_first = first;
+      s_nsrc = lo - first + 1;
+    }
+    __syncthreads();
+    const uint32_t first = s_first, nsrc = s_nsrc;
+    // per-source clipped ranges and chunk counts; each thread owns 8 sources
+    constexpr uint32_t PER = (kGatherTile + kGatherThreads - 1) / kGatherThreads;
+    uint32_t cnt[PER];
+    uint32_t part = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < PER; ++q) {
+      const uint32_t k = tid * PER + q;
+      cnt[q] = 0;
+      if (k < nsrc) {
+        const uint32_t i = first + k;
+        const uint32_t bp = ptr[i] - edge_from, be = ptr[i + 1] - edge_from;
+        const uint32_t lo = max(bp, j0), hi = min(be, j1);
+        const uint32_t hlo = off[queue[i]] + (lo - bp);
+        s_bpos[k] = lo;
+        s_hlo[k] = hlo;
+        s_len[k] = hi - lo;
+        cnt[q] = (hlo + (hi - lo) + R - 1) / R - hlo / R;
+        part += cnt[q];
+      }
+    }
+    // block scan of the per-thread partial sums
+    {
+      const int lane = tid & 31, warp = tid >> 5;
+      const uint32_t incl = warp_incl_scan(part, lane);
+      if (lane == 31) s_part[warp] = incl;
+      __syncthreads();
+      if (tid == 0) {
+        uint32_t acc = 0;
+        for (int w = 0; w < kGatherThreads / 32; ++w) { uint32_t x = s_part[w]; s_part[w] = acc; acc += x; }
+        s_part[kGatherThreads] = acc;
+      }
+      __syncthreads();
+      uint32_t run = s_part[warp] + incl - part;
+#pragma unroll
+      for (uint32_t q = 0; q < PER; ++q) {
+        const uint32_t k = tid * PER + q;
+        if (k < nsrc) { s_cs[k] = run; run += cnt[q]; }
+      }
+    }
+    __syncthreads();
+    const uint32_t total = s_part[kGatherThreads];
+    constexpr int U = 4;
+    for (uint32_t jb = tid; jb < total; jb += U * blockDim.x) {
+      uint4 v[U];
+      uint32_t kk[U], cc[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t j = jb + u * blockDim.x;
+        kk[u] = 0xffffffffu;
+        if (j < total) {
+          const uint32_t k = last_le(s_cs, nsrc, j);
+          const uint32_t c = s_hlo[k] / R + (j - s_cs[k]);
+          kk[u] = k;
+          cc[u] = c;
+          v[u] = host16[c];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (kk[u] == 0xffffffffu) continue;
+        const uint32_t k = kk[u];
+        const uint32_t hlo = s_hlo[k], len = s_len[k], bpos = s_bpos[k];
+        const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+        for (uint32_t r = 0; r < R; ++r) {
+          const uint32_t rec = cc[u] * R + r;
+          if (rec >= hlo && rec - hlo < len) {
+            const uint32_t o = bpos + (rec - hlo);
+            if (W == 1) buf[o] = w[r];
+            else reinterpret_cast<uint2 *>(buf)[o] = make_uint2(w[2 * r], w[2 * r + 1]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---- relaxation ----------------------------------------------------------------
 // Per-algorithm semiring (shared/gpu_kernels.cu): candidate value from the
 // source value and the edge, and whether it improves the destination.

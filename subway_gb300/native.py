@@ -21,6 +21,7 @@ INF = 4294967294
 OPT_PROFILE = 0x1
 OPT_NO_OVERLAP = 0x2
 OPT_NO_PACK = 0x4
+OPT_SCALAR_GATHER = 0x8
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
 MODES = {"sync": SYNC, "async": ASYNC}
 

@@ -228,10 +228,15 @@ def test_engine_matches_reference_golden(gpu):
 
 
 @pytest.mark.parametrize("mode", MODES)
-def test_reference_records_without_packing(gpu, orc, g12w, mode):
-    """SGW_OPT_NO_PACK moves the reference's 8-byte records; same answers."""
+@pytest.mark.parametrize("flags", ["NO_PACK", "SCALAR_GATHER", "NO_PACK|SCALAR_GATHER"])
+def test_transfer_forms(gpu, orc, g12w, mode, flags):
+    """8-byte records (SGW_OPT_NO_PACK) and the one-record-per-thread gather
+    (SGW_OPT_SCALAR_GATHER) give the same answers as the defaults."""
     g = g12w
-    eng = gpu.Engine(g, budget_bytes=18 * g.n + 72 * 1024 + 3000 * 16, flags=gpu.OPT_NO_PACK)
+    f = 0
+    for name in flags.split("|"):
+        f |= getattr(gpu, "OPT_" + name)
+    eng = gpu.Engine(g, budget_bytes=18 * g.n + 72 * 1024 + 3000 * 16, flags=f)
     src = int(g.pick_sources(1, seed=9)[0])
     for algo in ALGS:
         vals, _ = eng.run(algo, mode, src)
