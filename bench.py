@@ -64,6 +64,10 @@ def parse_args():
     ap.add_argument("--tile-degree-max", type=int, default=0)
     ap.add_argument("--chunk-edges", type=int, default=0)
     ap.add_argument("--inner-batch", type=int, default=0)
+    ap.add_argument("--policy", default="both", choices=["plain", "learned", "both"],
+                    help="both: time the plain (reference) schedule, then the learned one (headline)")
+    ap.add_argument("--model", default="", help="scheduler model file; 'none' = persistence predictor")
+    ap.add_argument("--num-buffers", type=int, default=3, help="edge buffers of the learned policy")
     return ap.parse_args()
 
 
@@ -199,24 +203,54 @@ def run_ours(a, dist):
     sources = g.pick_sources(a.sources, seed=a.seed)
     t_gen = time.time() - t0
     flags = N.OPT_PROFILE | (N.OPT_NO_PACK if a.no_pack else 0)
-    eng = N.Engine(g, budget_bytes=int(a.budget), device=dev, flags=flags, gather_ctas=a.gather_ctas,
-                   tile_degree_max=a.tile_degree_max, chunk_edges=a.chunk_edges, inner_batch=a.inner_batch)
     h2d_peak, d2h_peak = probe_link(N, dev)
     import numpy as np
-    out = np.empty(g.n, np.uint32)  # host result buffer
-    for k in range(a.warmup):
-        eng.run(a.algo, a.mode, int(sources[k % len(sources)]), out=out)
-    steps = []
-    dist.barrier()
-    with ClockSampler(dev) as clk:
-        t_start = time.perf_counter()
-        for k in range(a.steps):
-            t = time.perf_counter()
-            _, st = eng.run(a.algo, a.mode, int(sources[k % len(sources)]), out=out)
-            st["wall_ms"] = (time.perf_counter() - t) * 1e3
-            steps.append(st)
-        t_total = time.perf_counter() - t_start
-    dist.barrier()
+    out = np.empty(g.n, np.float32 if a.algo == "pr" else np.uint32)  # host result buffer
+
+    def engine(policy):
+        nb = a.num_buffers if policy == "learned" else 0
+        e = N.Engine(g, budget_bytes=int(a.budget), device=dev, flags=flags, gather_ctas=a.gather_ctas,
+                     tile_degree_max=a.tile_degree_max, chunk_edges=a.chunk_edges,
+                     inner_batch=a.inner_batch, num_buffers=nb)
+        if policy == "learned":
+            from subway_gb300 import scheduler
+            model = None if a.model == "none" else (N.Mlp.load(a.model, dev) if a.model else
+                                                     scheduler.load_default(dev))
+            e.set_policy("learned", model)
+            e.model_name = "persistence" if model is None else Path(a.model or scheduler.DEFAULT_MODEL).name
+        return e
+
+    def measure(eng):
+        for k in range(a.warmup):
+            eng.run(a.algo, a.mode, int(sources[k % len(sources)]), out=out)
+        steps = []
+        dist.barrier()
+        with ClockSampler(dev) as clk:
+            t_start = time.perf_counter()
+            for k in range(a.steps):
+                t = time.perf_counter()
+                _, st = eng.run(a.algo, a.mode, int(sources[k % len(sources)]), out=out)
+                st["wall_ms"] = (time.perf_counter() - t) * 1e3
+                steps.append(st)
+            t_total = time.perf_counter() - t_start
+        dist.barrier()
+        return steps, clk, t_total
+
+    plain_summary = None
+    if a.policy in ("plain", "both"):
+        eng = engine("plain")
+        steps, clk, t_total = measure(eng)
+        if a.policy == "both":
+            r = dist.sum(sum(s["reached_edges"] for s in steps))
+            plain_summary = {"value": round(r / (dist.max(sum(s["ms_device"] for s in steps)) * 1e6), 4),
+                             "e2e": round(r / (dist.max(sum(s["wall_ms"] for s in steps)) * 1e6), 4),
+                             "h2d_bytes_per_run": int(sum(s["h2d_bytes"] for s in steps) / a.steps),
+                             "ms_per_step": round(sum(s["ms_device"] for s in steps) / a.steps, 4),
+                             "iterations_per_step": round(sum(s["global_iterations"] for s in steps) / a.steps, 2)}
+            eng.close()
+    if a.policy in ("learned", "both"):
+        eng = engine("learned")
+        steps, clk, t_total = measure(eng)
     reached = sum(s["reached_edges"] for s in steps)
     dev_ms = sum(s["ms_device"] for s in steps)
     wall_ms = sum(s["wall_ms"] for s in steps)
@@ -265,8 +299,15 @@ def run_ours(a, dist):
         "metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": dist.world, "steps": K,
         "warmup": a.warmup, "ms_per_step": round(dev_ms_max / K, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": workload_config(a, {"policy": "plain",
+        "config": workload_config(a, {"policy": "plain" if a.policy == "plain" else "learned",
+                                      "scheduler_model": getattr(eng, "model_name", None),
+                                      "edge_buffers": a.num_buffers if a.policy != "plain" else 2,
                                       "transfer_record_bytes": 4 if (weighted and not a.no_pack) or not weighted else 8}),
+        "plain_policy": plain_summary,
+        "learned_over_plain": (None if not plain_summary else
+                               {"speedup": round(value / plain_summary["value"], 3),
+                                "e2e_speedup": round(e2e / plain_summary["e2e"], 3),
+                                "h2d_bytes_ratio": round(h2d / max(plain_summary["h2d_bytes_per_run"], 1), 3)}),
         "e2e": {"value": round(e2e, 4), "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(wall_ms_max / K, 4)},
         "h2d_bytes_per_run": int(h2d),

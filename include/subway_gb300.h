@@ -110,7 +110,9 @@ typedef struct sgw_engine_opts {
   uint32_t tile_degree_max;/* sources above this degree go to the chunk list  */
   uint32_t chunk_edges;    /* edges per chunk-list item (multiple of 32)      */
   uint32_t gather_ctas;    /* CTAs of the gather kernel, 0 = 2 per SM          */
-  uint32_t reserved[7];
+  uint32_t num_buffers;    /* device edge buffers sharing the budget, 0 = 2
+                              (1 with SGW_OPT_NO_OVERLAP), at most 8          */
+  uint32_t reserved[6];
 } sgw_engine_opts;
 
 void sgw_engine_opts_default(sgw_engine_opts *opts);
@@ -246,6 +248,116 @@ int sgw_plan_partitions(const uint32_t *ptr, uint32_t count, uint64_t cap,
 
 /* Number of CUDA devices visible (0 on a machine without a GPU). */
 int sgw_device_count(int *count);
+
+/* ---- learned scheduler ------------------------------------------------------
+ * No counterpart in the reference, whose only schedule is: compact every
+ * active vertex's edges, cut the queue greedily into budget-sized partitions,
+ * process them in vertex order, iterate each async partition to convergence
+ * (SGW_POLICY_PLAIN, the default, which this engine reproduces).
+ *
+ * SGW_POLICY_LEARNED cuts the vertex ids into static ranges that each fit one
+ * edge buffer.  After every generate step a kernel counts each range's active
+ * vertices and edges and evaluates the network below on five features
+ * (active vertex fraction, active edge fraction, growth of the active edges
+ * since the previous iteration, iteration index, range edge count), giving
+ * the predicted active edge fraction of the range in the next iteration.
+ * The host then, per active range: processes it from HBM if a buffer still
+ * holds it (no transfer); else streams the whole range (one DMA copy, and the
+ * buffer keeps it) when the extra bytes now are covered by the predicted
+ * bytes saved next iteration, or gathers only its active edges; evicts the
+ * buffer with the lowest predicted saving; and orders resident ranges first.
+ * Results are identical to the plain policy (the schedule changes, the
+ * fixpoint does not).  With model == NULL the prediction is the current
+ * active edge fraction.
+ *
+ * The network: 5 -> 64 -> 64 -> 1, ReLU, sigmoid output, BF16 weights, FP32
+ * accumulation, trained by binary cross-entropy with Adam on FP32 masters,
+ * all in hand-written kernels.  Parameters are flat FP32 arrays in the order
+ * W1[64][5], b1[64], W2[64][64], b2[64], W3[64], b3. */
+typedef struct sgw_mlp sgw_mlp;
+#define SGW_MLP_INPUTS 5
+#define SGW_MLP_HIDDEN 64
+#define SGW_MLP_PARAMS 4609
+#define SGW_POLICY_PLAIN 0
+#define SGW_POLICY_LEARNED 1
+
+int sgw_mlp_create(int device, uint64_t seed, sgw_mlp **out);
+int sgw_mlp_destroy(sgw_mlp *m);
+/* Sets the FP32 masters (and their BF16 copy) and resets the optimiser. */
+int sgw_mlp_set_params(sgw_mlp *m, const float *params);
+/* The BF16 weights the passes use, widened to FP32. */
+int sgw_mlp_get_params(const sgw_mlp *m, float *params);
+/* Host arrays: x is n x SGW_MLP_INPUTS, y and t have n entries. */
+int sgw_mlp_forward(sgw_mlp *m, const float *x, uint32_t n, float *y);
+int sgw_mlp_gradient(sgw_mlp *m, const float *x, const float *t, uint32_t n,
+                     float *grad, float *loss);
+int sgw_mlp_train(sgw_mlp *m, const float *x, const float *t, uint32_t n,
+                  uint32_t steps, float lr, float *loss);
+int sgw_mlp_save(const sgw_mlp *m, const char *path);
+int sgw_mlp_load(int device, const char *path, sgw_mlp **out);
+
+/* Takes effect from the next run; the model's weights are copied into the
+ * engine's device budget, so the model may be destroyed afterwards. */
+int sgw_set_policy(sgw_engine *e, int policy, const sgw_mlp *model);
+
+/* Per range and global iteration of a SGW_POLICY_LEARNED run (recorded while
+ * the trace is enabled): the features, the prediction and what was done. */
+#define SGW_ACT_SKIP 0      /* no active vertex                               */
+#define SGW_ACT_RESIDENT 1  /* processed from a buffer that still held it     */
+#define SGW_ACT_STREAM 2    /* whole range copied, kept resident              */
+#define SGW_ACT_COMPACT 3   /* active edges gathered                          */
+#define SGW_ACT_SPLIT 4     /* one vertex larger than a buffer, in pieces     */
+typedef struct sgw_range_rec {
+  uint32_t global_iteration;
+  uint32_t range;
+  uint32_t active_nodes;
+  uint32_t range_nodes;
+  uint32_t active_edges;
+  uint32_t range_edges;
+  uint32_t action;
+  uint32_t inner_iterations;
+  float features[5];
+  float predicted;
+  uint64_t bytes_h2d;
+} sgw_range_rec;
+int sgw_range_trace_count(const sgw_engine *e, uint64_t *count);
+int sgw_range_trace_read(const sgw_engine *e, sgw_range_rec *out, uint64_t capacity,
+                         uint64_t *count);
+
+/* ---- batched multi-source queries ------------------------------------------
+ * No counterpart in the reference, which runs one source per process
+ * (subway/bfs-sync.cu, subway/sssp-sync.cu).  Up to 64 BFS or SSSP queries
+ * share one traversal of a graph held in HBM: per vertex one distance per
+ * query lane and a 64-bit lane mask for the current and next frontier.  A
+ * batch is one CUDA-graph launch whose conditional WHILE node repeats the
+ * frontier/relax iteration on the device until no lane improves.  Results
+ * are bit-exact with single-source runs.
+ * opts: budget_bytes (admission: SGW_EBUDGET if the graph, lanes x n
+ * distances and the work lists do not fit), device, chunk_edges (edges per
+ * work item, default 256), flags (SGW_OPT_NO_PACK). */
+typedef struct sgw_batch sgw_batch;
+typedef struct sgw_batch_stats {
+  uint32_t iterations;      /* frontier iterations of the batch               */
+  uint32_t queries;
+  double ms_device;         /* CUDA-event time of the traversal               */
+  double ms_wall;           /* the whole call, results copied to the host     */
+  uint64_t d2h_bytes;
+  uint64_t reserved[4];
+} sgw_batch_stats;
+
+/* lanes: 32 or 64 (the widest batch). */
+int sgw_batch_create(const sgw_graph *g, const sgw_engine_opts *opts, uint32_t lanes,
+                     sgw_batch **out);
+int sgw_batch_destroy(sgw_batch *b);
+int sgw_batch_device_bytes(const sgw_batch *b, uint64_t *bytes);
+/* algo: SGW_BFS or SGW_SSSP.  out: host array of nsrc x n uint32, query i's
+ * distances at out[i * n .. i * n + n); NULL leaves them in the batch's own
+ * pinned buffer (faster: no pageable copy), see sgw_batch_results. */
+int sgw_batch_run(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc,
+                  uint32_t *out, sgw_batch_stats *stats);
+/* The batch's pinned result buffer (lanes x n, lane-major), valid until the
+ * next sgw_batch_run or sgw_batch_destroy. */
+int sgw_batch_results(const sgw_batch *b, const uint32_t **results);
 
 /* ---- allocation-free compaction ------------------------------------------
  * No counterpart in the reference (its generate step allocates its scan

@@ -59,11 +59,11 @@ def _run_parallel(cmds, verbose=False):
 
 
 def lib_sources():
-    return [CSRC / "sgw_engine.cu", CSRC / "sgw_graph.cpp"]
+    return [CSRC / "sgw_engine.cu", CSRC / "sgw_mlp.cu", CSRC / "sgw_batch.cu", CSRC / "sgw_graph.cpp"]
 
 
 def lib_deps():
-    return lib_sources() + [CSRC / "sgw_kernels.cuh", CSRC / "sgw_internal.h",
+    return lib_sources() + [CSRC / "sgw_kernels.cuh", CSRC / "sgw_internal.h", CSRC / "sgw_mlp.cuh",
                             INCLUDE / "subway_gb300.h", INCLUDE / "sgw_graphgen.h"]
 
 
@@ -73,17 +73,17 @@ def build_lib(verbose=False, force=False) -> Path:
     LIBDIR.mkdir(exist_ok=True)
     OBJDIR.mkdir(exist_ok=True)
     nv = nvcc()
-    o_cu = OBJDIR / "sgw_engine.o"
+    cu = [CSRC / "sgw_engine.cu", CSRC / "sgw_mlp.cu", CSRC / "sgw_batch.cu"]
+    objs = [OBJDIR / (p.stem + ".o") for p in cu]
     o_cpp = OBJDIR / "sgw_graph.o"
-    cmds = [
-        [nv, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-         f"-I{INCLUDE}", "-c", CSRC / "sgw_engine.cu", "-o", o_cu],
-        ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", f"-I{INCLUDE}",
-         "-c", CSRC / "sgw_graph.cpp", "-o", o_cpp],
-    ]
+    cmds = [[nv, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+             f"-I{INCLUDE}", "-c", src, "-o", obj] for src, obj in zip(cu, objs)]
+    cmds.append(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", f"-I{INCLUDE}",
+                 "-c", CSRC / "sgw_graph.cpp", "-o", o_cpp])
     _run_parallel(cmds, verbose)
     tmp = LIB.with_suffix(".so.tmp")
-    _run_parallel([[nv, *ARCH, "-shared", o_cu, o_cpp, "-o", tmp, "-Xcompiler", "-fopenmp", "-lgomp"]], verbose)
+    _run_parallel([[nv, *ARCH, "-shared", *objs, o_cpp, "-o", tmp, "-Xcompiler", "-fopenmp", "-lgomp"]],
+                  verbose)
     os.replace(tmp, LIB)
     return LIB
 

@@ -40,6 +40,8 @@ struct ProfEvent {
   cudaEvent_t a, b;
 };
 
+constexpr int kMaxBuf = 8;  // edge buffers an engine can hold
+
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 }  // namespace
@@ -58,14 +60,19 @@ struct sgw_engine {
   uint32_t *d_off = nullptr;
   uint32_t *d_value = nullptr;
   uint8_t *d_l1 = nullptr, *d_l2 = nullptr;
+  uint32_t *d_dq[2] = {nullptr, nullptr};  // async dirty lists (ping-pong)
+  uint32_t dq_cap = 0;
   uint32_t *d_queue = nullptr, *d_ptr = nullptr;
   uint32_t *d_tflag = nullptr;
   unsigned long long *d_tagg = nullptr, *d_tincl = nullptr;
   Ctl *d_ctl = nullptr;
   Part *d_parts = nullptr;
   WorkItem *d_wl = nullptr;
-  uint32_t *d_buf[2] = {nullptr, nullptr};
+  uint32_t *d_buf[kMaxBuf] = {};
   double *d_pval = nullptr, *d_delta = nullptr, *d_qpush = nullptr;  // PR family
+  __nv_bfloat16 *d_mlp = nullptr;          // scheduler weights (learned policy)
+  RangeInfo *d_ranges = nullptr;           // static vertex ranges of this family
+  RangeStat *d_rstat = nullptr;            // per-range statistics, one iteration
   int fam = 0;
   uint64_t cap_fam[2] = {0, 0};  // edge-buffer capacity of each family in this arena
   uint64_t cap = 0;  // edges per buffer
@@ -82,9 +89,11 @@ struct sgw_engine {
   size_t packed_bytes = 0;
   bool packed_registered = false;
   bool vec_gather = false;                 // host records readable as aligned 16-B words
+  uint32_t cur_streamed = 0;               // partition being relaxed: whole-range buffer
+  uint32_t cur_stream_base = 0;            //   and the first edge of that range
   uint32_t pbits = 0;                      // packed: bits of the destination id
   cudaStream_t s_comp = nullptr, s_copy = nullptr;
-  cudaEvent_t ev_ready[2] = {}, ev_free[2] = {};
+  cudaEvent_t ev_ready[kMaxBuf] = {}, ev_free[kMaxBuf] = {};
   cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
   std::vector<ProfEvent> prof;
   size_t prof_used = 0;
@@ -101,6 +110,14 @@ struct sgw_engine {
   sgw_run_stats stats{};
   bool trace_on = false;
   std::vector<sgw_trace_rec> trace;
+
+  // learned policy
+  int policy = SGW_POLICY_PLAIN;
+  bool have_model = false;                 // d_mlp holds trained weights
+  std::vector<RangeInfo> ranges;           // host copy of the static ranges
+  RangeStat *h_rstat = nullptr;            // pinned, max_parts entries
+  int buf_range[kMaxBuf];                  // range a buffer holds whole, or -1
+  std::vector<sgw_range_rec> rtrace;
 };
 
 namespace {
@@ -169,9 +186,10 @@ int read_ctl(sgw_engine *e) {
 enum Family { FAM_INT = 0, FAM_PR = 1 };
 
 struct Layout {
-  size_t off, tflag, tagg, tincl, ctl;                // common
+  size_t off, tflag, tagg, tincl, ctl, mlp;           // common
   size_t value, l1, l2, queue, ptr, delta, qpush;     // family
-  size_t parts, wl, buf0, buf1, total;
+  size_t parts, ranges, rstat, wl, dq0, dq1, buf[kMaxBuf], total;
+  uint32_t dq_cap;
   uint64_t cap;
   uint32_t max_parts, wl_cap;
 };
@@ -186,6 +204,7 @@ Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
   L.tagg = take(8ull * num_tiles);
   L.tincl = take(8ull * num_tiles);
   L.ctl = take(sizeof(Ctl));
+  L.mlp = take(sizeof(__nv_bfloat16) * kMlpParams);
   if (fam == FAM_INT) {
     L.value = take(4ull * n);
     L.l1 = take(n);
@@ -197,14 +216,19 @@ Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
   L.queue = take(4ull * n);
   L.ptr = take(4ull * (n + 1));
   if (fam == FAM_PR) L.qpush = take(8ull * n);
+  // async dirty lists: n / 8 entries each (overflow falls back to a scan)
+  L.dq_cap = fam == FAM_INT ? std::max<uint32_t>(4096u, n / 8) : 0u;
+  L.dq0 = take(4ull * L.dq_cap);
+  L.dq1 = take(4ull * L.dq_cap);
   L.cap = cap;
   L.max_parts = (uint32_t)std::min<uint64_t>(2ull * ((uint64_t)m / std::max<uint64_t>(cap, 1) + 1) + 2,
                                              0x7fffffffull);
   L.wl_cap = (uint32_t)std::min<uint64_t>(cap / chunk + cap / std::max<uint32_t>(tdm, 1) + 64, 0x7fffffffull);
   L.parts = take(sizeof(Part) * (size_t)L.max_parts);
+  L.ranges = take(sizeof(RangeInfo) * (size_t)L.max_parts);
+  L.rstat = take(sizeof(RangeStat) * (size_t)L.max_parts);
   L.wl = take(16ull * (size_t)L.wl_cap);  // WorkItem and PrItem are 16 B
-  L.buf0 = take(cap * esz);
-  L.buf1 = nbuf > 1 ? take(cap * esz) : L.buf0;
+  for (uint32_t b = 0; b < kMaxBuf; ++b) L.buf[b] = b < nbuf ? take(cap * esz) : L.buf[0];
   L.total = p;
   return L;
 }
@@ -212,19 +236,26 @@ Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
 // Largest edge-buffer capacity whose layout fits `bytes` (0 if none does).
 uint64_t fit_cap(int fam, const sgw_engine_opts &o, uint32_t n, uint32_t m, uint32_t esz,
                  uint32_t nbuf, uint32_t num_tiles, uint64_t bytes) {
-  const Layout L0 = make_layout(fam, n, m, esz, nbuf, num_tiles, 64, o.chunk_edges, o.tile_degree_max);
-  if (L0.total > bytes) return 0;
-  const double per_edge = (double)nbuf * esz + 16.0 / o.chunk_edges + 16.0 / o.tile_degree_max +
-                          2.0 * sizeof(Part) / 64.0;
-  uint64_t cap = (uint64_t)((double)(bytes - L0.total) / per_edge) + 64;
-  cap = std::min<uint64_t>(cap, std::max<uint64_t>(m, 64));
-  cap = std::min<uint64_t>(cap, 4294967294ull);  // max_partition_size <= DIST_INFINITY
-  while (cap > 64 && make_layout(fam, n, m, esz, nbuf, num_tiles, cap, o.chunk_edges,
-                                 o.tile_degree_max).total > bytes)
-    cap -= std::max<uint64_t>(cap / 64, 64);
-  if (cap < 64) cap = 64;
-  return make_layout(fam, n, m, esz, nbuf, num_tiles, cap, o.chunk_edges, o.tile_degree_max).total <= bytes
-             ? cap : 0;
+  auto total = [&](uint64_t cap) {
+    return (uint64_t)make_layout(fam, n, m, esz, nbuf, num_tiles, cap, o.chunk_edges, o.tile_degree_max).total;
+  };
+  // max_partition_size <= DIST_INFINITY, and no larger than the whole graph
+  const uint64_t hi_cap = std::min<uint64_t>(std::max<uint64_t>(m, 64), 4294967294ull);
+  // The layout is convex in cap: the partition/range tables shrink as 1/cap,
+  // the buffers grow as cap.  Below the minimum nothing fits; above it the
+  // size grows monotonically, so bisect for the largest cap that fits.
+  const double table = 2.0 * m * (sizeof(Part) + sizeof(RangeInfo) + sizeof(RangeStat));
+  const double per_edge = (double)nbuf * esz + 16.0 / o.chunk_edges + 16.0 / o.tile_degree_max;
+  uint64_t lo = std::max<uint64_t>(64, (uint64_t)std::sqrt(table / per_edge));
+  lo = std::min(lo, hi_cap);
+  if (total(lo) > bytes) return 0;
+  if (total(hi_cap) <= bytes) return hi_cap;
+  uint64_t a = lo, b = hi_cap;  // total(a) fits, total(b) does not
+  while (b - a > 1) {
+    const uint64_t mid = a + (b - a) / 2;
+    if (total(mid) <= bytes) a = mid; else b = mid;
+  }
+  return a;
 }
 
 int carve(sgw_engine *e, int fam, uint64_t cap) {
@@ -240,19 +271,53 @@ int carve(sgw_engine *e, int fam, uint64_t cap) {
   e->d_value = (uint32_t *)(b + L.value);
   e->d_l1 = fam == FAM_INT ? (uint8_t *)(b + L.l1) : nullptr;
   e->d_l2 = fam == FAM_INT ? (uint8_t *)(b + L.l2) : nullptr;
+  e->d_dq[0] = L.dq_cap ? (uint32_t *)(b + L.dq0) : nullptr;
+  e->d_dq[1] = L.dq_cap ? (uint32_t *)(b + L.dq1) : nullptr;
+  e->dq_cap = L.dq_cap;
   e->d_pval = fam == FAM_PR ? (double *)(b + L.value) : nullptr;
   e->d_delta = fam == FAM_PR ? (double *)(b + L.delta) : nullptr;
   e->d_qpush = fam == FAM_PR ? (double *)(b + L.qpush) : nullptr;
   e->d_queue = (uint32_t *)(b + L.queue);
   e->d_ptr = (uint32_t *)(b + L.ptr);
   e->d_parts = (Part *)(b + L.parts);
+  e->d_ranges = (RangeInfo *)(b + L.ranges);
+  e->d_rstat = (RangeStat *)(b + L.rstat);
+  e->d_mlp = (__nv_bfloat16 *)(b + L.mlp);
   e->d_wl = (WorkItem *)(b + L.wl);
-  e->d_buf[0] = (uint32_t *)(b + L.buf0);
-  e->d_buf[1] = (uint32_t *)(b + L.buf1);
+  for (int i = 0; i < kMaxBuf; ++i) e->d_buf[i] = (uint32_t *)(b + L.buf[i]);
   e->cap = L.cap;
   e->max_parts = L.max_parts;
   e->wl_cap = L.wl_cap;
   e->fam = fam;
+  // static vertex ranges: greedy runs of whole vertices whose edges fit one
+  // buffer; a vertex above the buffer is a range of its own
+  e->ranges.clear();
+  const uint32_t *np = e->g->node_pointer;
+  for (uint32_t v = 0; v < e->n;) {
+    const uint64_t limit = (uint64_t)np[v] + e->cap;
+    uint32_t lo = v + 1, hi = e->n + 1;  // first index in (v, n] with np > limit
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if ((uint64_t)np[mid] <= limit) lo = mid + 1; else hi = mid;
+    }
+    uint32_t v1 = lo - 1;
+    if (v1 <= v) v1 = v + 1;
+    e->ranges.push_back(RangeInfo{v, v1, np[v], np[v1]});
+    v = v1;
+  }
+  if (e->ranges.size() > e->max_parts) return fail(SGW_ERANGE, "too many vertex ranges");
+  for (int i = 0; i < kMaxBuf; ++i) e->buf_range[i] = -1;
+  return SGW_OK;
+}
+
+int generate_and_stats(sgw_engine *e, int consume);
+
+// Copies the range table to the device (after carving, on the compute stream).
+int upload_ranges(sgw_engine *e) {
+  if (!e->ranges.empty())
+    CK(cudaMemcpyAsync(e->d_ranges, e->ranges.data(), sizeof(RangeInfo) * e->ranges.size(),
+                       cudaMemcpyHostToDevice, e->s_comp));
+  CK(cudaMemsetAsync(e->d_rstat, 0, sizeof(RangeStat) * e->max_parts, e->s_comp));
   return SGW_OK;
 }
 
@@ -350,10 +415,17 @@ void trace_partition(sgw_engine *e, uint32_t p, uint32_t inner) {
   e->trace.push_back(r);
 }
 
+int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s);
+
 int enqueue_gather(sgw_engine *e, uint32_t p, cudaStream_t s) {
   const Part &q = e->h_parts[p];
-  const uint32_t b = p % e->nbuf;
   if (is_hub(e, q) || q.edge_count == 0) return SGW_OK;
+  return gather_into(e, q, p % e->nbuf, s);
+}
+
+// Gathers partition q's active edges into buffer b on stream s, after the
+// buffer's last reader, and records ev_ready[b].
+int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
   CK(cudaStreamWaitEvent(s, e->ev_free[b], 0));
   size_t slot = 0;
   TRY(prof_begin(e, K_GATHER, s, &slot));
@@ -403,6 +475,14 @@ int launch_relax_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, u
   a.tile_degree_max = e->opts.tile_degree_max;
   a.chunk_edges = e->opts.chunk_edges;
   a.pbits = e->pbits;
+  a.streamed = e->cur_streamed;
+  a.stream_base = e->cur_stream_base;
+  a.off = e->d_off;
+  a.dq_in = (ASYNC && iter > 1) ? e->d_dq[(iter - 1) & 1u] : nullptr;
+  a.dq_out = e->d_dq[iter & 1u];
+  a.dq_cap = e->dq_cap;
+  a.v_lo = q.first_vertex;
+  a.v_hi = q.last_vertex;
   const uint32_t g1 = grid_for(e, q.size, kRelaxThreads);
   k_relax_tile<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
   CK(cudaGetLastError());
@@ -446,6 +526,9 @@ int launch_pr_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter) {
   a.tile_degree_max = e->opts.tile_degree_max;
   a.chunk_edges = e->opts.chunk_edges;
   a.pbits = e->pbits;
+  a.streamed = e->cur_streamed;
+  a.stream_base = e->cur_stream_base;
+  a.off = e->d_off;
   a.acc = (double)e->params.pr_acc;
   a.damping = (double)e->params.pr_damping;
   k_pr_tile<ASYNC, W><<<grid_for(e, q.size, kRelaxThreads), kRelaxThreads, 0, e->s_comp>>>(a);
@@ -532,7 +615,8 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
 // then inner iterations until no relaxation improves (or max_inner).
 int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_out) {
   const bool async = e->params.mode == SGW_ASYNC;
-  CK(cudaMemsetAsync(&e->d_ctl->upd[0], 0, sizeof(uint32_t) * 9, e->s_comp));  // upd, wl_count, iters_run
+  // upd, wl_count, iters_run, dq_count, dq_overflow
+  CK(cudaMemsetAsync(&e->d_ctl->upd[0], 0, sizeof(uint32_t) * 17, e->s_comp));
   if (!async) {
     size_t slot = 0;
     TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
@@ -591,8 +675,12 @@ int state_init(sgw_engine *e, const sgw_run_params *p) {
   e->initialized = false;
   e->gitr = 0;
   e->trace.clear();
+  e->rtrace.clear();
   const int fam = p->algo == SGW_PR ? FAM_PR : FAM_INT;
   if (fam != e->fam) TRY(carve(e, fam, e->cap_fam[fam]));
+  // every run starts with empty edge buffers (nothing carried between runs)
+  for (int i = 0; i < kMaxBuf; ++i) e->buf_range[i] = -1;
+  if (e->policy == SGW_POLICY_LEARNED) TRY(upload_ranges(e));
   const uint32_t src = (p->algo == SGW_CC || p->algo == SGW_PR) ? 0xffffffffu : p->source;
   if (fam == FAM_PR)
     k_pr_init<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, (double)p->pr_init, e->d_pval, e->d_delta);
@@ -603,7 +691,8 @@ int state_init(sgw_engine *e, const sgw_run_params *p) {
   CK(cudaMemsetAsync(e->d_ctl, 0, sizeof(Ctl), e->s_comp));
   e->stats.launches += 1;
   const bool async = p->mode == SGW_ASYNC;
-  TRY(generate_and_plan(e, async ? 0 : 1));
+  if (e->policy == SGW_POLICY_LEARNED) TRY(generate_and_stats(e, async ? 0 : 1));
+  else TRY(generate_and_plan(e, async ? 0 : 1));
   if (async && p->algo != SGW_CC && p->algo != SGW_PR) {
     k_async_reset<<<grid_for(e, e->n, 256), 256, 0, e->s_comp>>>(e->n, p->source, e->d_l1);
     CK(cudaGetLastError());
@@ -634,6 +723,189 @@ int process_iteration(sgw_engine *e) {
     trace_partition(e, p, inner);
     if (e->nbuf == 1 && p + 1 < P) TRY(enqueue_gather(e, p + 1, e->s_copy));
     e->stats.partitions += 1;
+  }
+  return SGW_OK;
+}
+
+// ---- learned policy ------------------------------------------------------------
+// generate + per-range statistics and predictions + one read-back.
+int generate_and_stats(sgw_engine *e, int consume) {
+  TRY(launch_generate(e, consume));
+  const uint32_t S = (uint32_t)e->ranges.size();
+  const __nv_bfloat16 *w = e->have_model ? e->d_mlp : nullptr;
+  size_t slot = 0;
+  TRY(prof_begin(e, K_PLAN, e->s_comp, &slot));
+  k_range_stats<<<(S * 32 + 255) / 256, 256, 0, e->s_comp>>>(
+      e->d_ranges, S, e->d_queue, e->d_ptr, e->d_ctl, e->d_rstat, w, e->gitr + 1,
+      (uint32_t)std::min<uint64_t>(e->cap, 0xffffffffull));
+  CK(cudaGetLastError());
+  TRY(prof_end(e, e->s_comp, slot));
+  e->stats.launches += 1;
+  CK(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
+  CK(cudaMemcpyAsync(e->h_rstat, e->d_rstat, sizeof(RangeStat) * S, cudaMemcpyDeviceToHost, e->s_comp));
+  CK(cudaStreamSynchronize(e->s_comp));
+  TRY(check_ctl_error(e));
+  e->num_active = e->h_ctl->num_active;
+  e->num_active_edges = e->h_ctl->num_active_edges;
+  e->stats.d2h_bytes += sizeof(Ctl) + sizeof(RangeStat) * S;
+  e->parts_valid = false;
+  return SGW_OK;
+}
+
+struct Job {
+  uint32_t s;       // range
+  uint32_t action;  // SGW_ACT_*
+  int buf = -1;     // buffer it is processed from
+  bool ready = false;
+};
+
+Part range_part(const RangeStat &st) {
+  Part q;
+  q.from = st.qa;
+  q.size = st.qb - st.qa;
+  q.edge_from = st.edge_from;
+  q.first_vertex = st.first_vertex;
+  q.last_vertex = st.last_vertex;
+  q.pad = 0;
+  q.edge_count = st.act_edges;
+  return q;
+}
+
+// Enqueues job j's transfer into buffer b on the copy stream.
+int range_transfer(sgw_engine *e, Job &j, int b) {
+  const RangeInfo &r = e->ranges[j.s];
+  const RangeStat &st = e->h_rstat[j.s];
+  if (j.action == SGW_ACT_STREAM) {
+    const size_t esz = 4ull * e->W;
+    const size_t bytes = (size_t)(r.e1 - r.e0) * esz;
+    CK(cudaStreamWaitEvent(e->s_copy, e->ev_free[b], 0));
+    size_t slot = 0;
+    TRY(prof_begin(e, K_GATHER, e->s_copy, &slot));
+    // a whole range is contiguous: one DMA copy, no SM time taken from the
+    // relaxation running on the compute stream
+    CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->h_src + (size_t)r.e0 * esz, bytes,
+                       cudaMemcpyHostToDevice, e->s_copy));
+    TRY(prof_end(e, e->s_copy, slot));
+    CK(cudaEventRecord(e->ev_ready[b], e->s_copy));
+    e->stats.h2d_bytes += bytes;
+    e->buf_range[b] = (int)j.s;
+  } else {
+    TRY(gather_into(e, range_part(st), (uint32_t)b, e->s_copy));
+    e->buf_range[b] = -1;
+  }
+  j.buf = b;
+  j.ready = true;
+  return SGW_OK;
+}
+
+// All active ranges of one global iteration under the learned policy.
+int process_iteration_ranges(sgw_engine *e) {
+  const uint32_t S = (uint32_t)e->ranges.size();
+  const uint32_t esz = 4 * e->W;
+  std::vector<int> held(S, -1);
+  for (uint32_t b = 0; b < e->nbuf; ++b)
+    if (e->buf_range[b] >= 0) held[e->buf_range[b]] = (int)b;
+  std::vector<Job> jobs;
+  std::vector<uint32_t> act(S, SGW_ACT_SKIP);
+  for (uint32_t s = 0; s < S; ++s) {  // resident ranges first: no transfer to wait for
+    const RangeStat &st = e->h_rstat[s];
+    if (st.qb > st.qa && held[s] >= 0) {
+      Job j;
+      j.s = s;
+      j.action = act[s] = SGW_ACT_RESIDENT;
+      j.buf = held[s];
+      j.ready = true;
+      jobs.push_back(j);
+    }
+  }
+  for (uint32_t s = 0; s < S; ++s) {
+    const RangeStat &st = e->h_rstat[s];
+    if (st.qb <= st.qa || held[s] >= 0) continue;
+    const RangeInfo &r = e->ranges[s];
+    const double E = (double)(r.e1 - r.e0), A = (double)st.act_edges;
+    Job j;
+    j.s = s;
+    if (E > (double)e->cap) j.action = SGW_ACT_SPLIT;
+    else if (E - A <= (double)st.pred * E) j.action = SGW_ACT_STREAM;  // extra bytes now <= predicted saving
+    else j.action = SGW_ACT_COMPACT;
+    act[s] = j.action;
+    jobs.push_back(j);
+  }
+  // keep value of a buffer: predicted bytes it saves next iteration
+  auto value = [&](uint32_t b) -> double {
+    const int r = e->buf_range[b];
+    if (r < 0) return -1.0;
+    return (double)e->h_rstat[r].pred * (double)(e->ranges[r].e1 - e->ranges[r].e0);
+  };
+  // a victim is not used by any job not yet enqueued and is not `exclude`
+  auto victim = [&](size_t from_job, int exclude) -> int {
+    int best = -1;
+    for (uint32_t b = 0; b < e->nbuf; ++b) {
+      if ((int)b == exclude) continue;
+      bool used = false;
+      for (size_t k = from_job; k < jobs.size() && !used; ++k) used = jobs[k].buf == (int)b;
+      if (used) continue;
+      if (best < 0 || value(b) < value((uint32_t)best)) best = (int)b;
+    }
+    return best;
+  };
+  std::vector<uint32_t> inner_of(S, 0);
+  for (size_t k = 0; k < jobs.size(); ++k) {
+    Job &j = jobs[k];
+    if (!j.ready && j.action != SGW_ACT_SPLIT) {
+      const int b = victim(k, -1);
+      if (b < 0) return fail(SGW_ESTATE, "no edge buffer free");
+      TRY(range_transfer(e, j, b));
+    }
+    if (k + 1 < jobs.size()) {  // prefetch the next transfer behind this relaxation
+      Job &nx = jobs[k + 1];
+      if (!nx.ready && nx.action != SGW_ACT_SPLIT) {
+        const int b = victim(k + 1, j.buf);
+        if (b >= 0) TRY(range_transfer(e, nx, b));
+      }
+    }
+    const RangeInfo &r = e->ranges[j.s];
+    const Part q = range_part(e->h_rstat[j.s]);
+    uint32_t inner = 1;
+    if (j.action == SGW_ACT_SPLIT) {
+      const int b = victim(k, -1);
+      if (b < 0) return fail(SGW_ESTATE, "no edge buffer free");
+      j.buf = b;
+      e->buf_range[b] = -1;
+      CK(cudaStreamWaitEvent(e->s_comp, e->ev_free[b], 0));
+      TRY(process_hub(e, q, (uint32_t)b));
+    } else {
+      CK(cudaStreamWaitEvent(e->s_comp, e->ev_ready[j.buf], 0));
+      e->cur_streamed = (j.action == SGW_ACT_RESIDENT || j.action == SGW_ACT_STREAM) ? 1u : 0u;
+      e->cur_stream_base = r.e0;
+      const int st = process_resident(e, q, (uint32_t)j.buf, &inner);
+      e->cur_streamed = 0;
+      TRY(st);
+    }
+    CK(cudaEventRecord(e->ev_free[j.buf], e->s_comp));
+    inner_of[j.s] = inner;
+    e->stats.partitions += 1;
+  }
+  if (e->trace_on) {
+    for (uint32_t s = 0; s < S; ++s) {
+      const RangeStat &st = e->h_rstat[s];
+      const RangeInfo &r = e->ranges[s];
+      sgw_range_rec rec;
+      memset(&rec, 0, sizeof(rec));
+      rec.global_iteration = e->gitr;
+      rec.range = s;
+      rec.active_nodes = st.qb - st.qa;
+      rec.range_nodes = r.v1 - r.v0;
+      rec.active_edges = st.act_edges;
+      rec.range_edges = r.e1 - r.e0;
+      rec.action = act[s];
+      rec.inner_iterations = inner_of[s];
+      for (int f = 0; f < 5; ++f) rec.features[f] = st.feat[f];
+      rec.predicted = st.pred;
+      rec.bytes_h2d = act[s] == SGW_ACT_STREAM ? (uint64_t)(r.e1 - r.e0) * esz
+                      : act[s] == SGW_ACT_COMPACT || act[s] == SGW_ACT_SPLIT ? (uint64_t)st.act_edges * esz : 0;
+      e->rtrace.push_back(rec);
+    }
   }
   return SGW_OK;
 }
@@ -746,14 +1018,15 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   e->n = g->n;
   e->m = g->m;
   e->W = g->weighted ? 2 : 1;
-  e->h_src = g->edges;
   // weighted records travel as one packed word when (w << bits(n)) | dst fits
-  if (g->weighted && !(o.flags & SGW_OPT_NO_PACK) &&
-      pack_weighted(g, &e->h_packed, &e->packed_bytes, &e->pbits)) {
-    e->W = 1;
-    e->h_src = e->h_packed;
-  }
+  bool pack = g->weighted && !(o.flags & SGW_OPT_NO_PACK) && pack_bits(g, &e->pbits);
+  if (pack) e->W = 1;
+  else e->pbits = 0;
   e->nbuf = (o.flags & SGW_OPT_NO_OVERLAP) ? 1 : 2;
+  if (o.num_buffers) {
+    if (o.num_buffers > (uint32_t)kMaxBuf) { delete e; return fail(SGW_EINVAL, "num_buffers above %d", kMaxBuf); }
+    e->nbuf = o.num_buffers;
+  }
   e->num_tiles = (uint32_t)((g->n + kGenTile - 1) / kGenTile);
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, o.device) != cudaSuccess) { delete e; return fail(SGW_ECUDA, "device properties"); }
@@ -770,19 +1043,20 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   if (budget == 0) {
     // Subway's rule: 0.9 * (totalGlobalMem - 32 n) bytes of edges
     // (shared/subgraph.cu:24), here on top of the engine's own vertex state.
-    const Layout L0 = make_layout(FAM_PR, e->n, e->m, esz, e->nbuf, e->num_tiles, 64,
+    const Layout L0 = make_layout(FAM_PR, e->n, e->m, esz, e->nbuf, e->num_tiles, mfull,
                                   o.chunk_edges, o.tile_degree_max);
+    const double state = (double)L0.total - (double)e->nbuf * mfull * esz;  // all but the buffers
     double edges_bytes = 0.9 * ((double)prop.totalGlobalMem - 32.0 * e->n);
-    budget = (uint64_t)(L0.total + std::max(0.0, edges_bytes));
+    budget = (uint64_t)(state + std::max(0.0, edges_bytes));
   }
   const size_t arena = (size_t)std::min<uint64_t>(budget, need);
   for (int fam = 0; fam < 2; ++fam)
     e->cap_fam[fam] = fit_cap(fam, o, e->n, e->m, esz, e->nbuf, e->num_tiles, arena);
   if (e->cap_fam[FAM_INT] == 0) {
-    const Layout L0 = make_layout(FAM_INT, e->n, e->m, esz, e->nbuf, e->num_tiles, 64,
+    const Layout L0 = make_layout(FAM_INT, e->n, e->m, esz, e->nbuf, e->num_tiles, 4096,
                                   o.chunk_edges, o.tile_degree_max);
     delete e;
-    return fail(SGW_EBUDGET, "budget %llu B < vertex state and minimum edge buffers (%zu B)",
+    return fail(SGW_EBUDGET, "budget %llu B < vertex state and minimum edge buffers (about %zu B)",
                 (unsigned long long)budget, L0.total);
   }
   e->budget = budget;
@@ -801,40 +1075,37 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
 
   int st = SGW_OK;
   auto cleanup = [&](int s) { sgw_engine_destroy(e); return s; };
-  // host edges readable by device kernels (mapped pinned memory)
-  const size_t ebytes = std::max<size_t>((size_t)e->m * esz, 4);
-  if (g->m > 0 && e->h_packed) {
-    ce = cudaHostRegister(e->h_packed, e->packed_bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
-    if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostRegister: %s", cudaGetErrorString(ce))); }
-    e->packed_registered = true;
+  // The transfer copy: the edge records (packed when they fit) in pinned,
+  // mapped host memory from cudaHostAlloc, read in place by the gather
+  // kernels and by DMA copies.  Registering the caller's pages instead makes
+  // DMA from them several times slower on the C2C-attached host.  16 bytes of
+  // padding let the 16-byte vector reads run past the last record.
+  if (g->m > 0) {
+    const size_t rec_bytes = (size_t)e->m * 4 * e->W;
+    e->packed_bytes = (rec_bytes + 16 + 15) / 16 * 16;
+    ce = cudaHostAlloc((void **)&e->h_packed, e->packed_bytes, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (ce != cudaSuccess) {
+      cudaGetLastError();
+      e->h_packed = nullptr;
+      return cleanup(fail(SGW_ECUDA, "cudaHostAlloc(%zu) for the transfer copy: %s", e->packed_bytes,
+                          cudaGetErrorString(ce)));
+    }
+    e->packed_registered = true;  // owned by the CUDA runtime: cudaFreeHost on destroy
+    if (pack) pack_into(g, e->pbits, e->h_packed);
+    else copy_records(g, e->h_packed);
+    memset((char *)e->h_packed + rec_bytes, 0, e->packed_bytes - rec_bytes);
+    e->h_src = e->h_packed;
     void *dp = nullptr;
     ce = cudaHostGetDevicePointer(&dp, e->h_packed, 0);
     if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce))); }
     e->d_host_edges = (const uint32_t *)dp;
-  } else if (g->m > 0) {
-    size_t reg_bytes = g->owns ? g->edges_bytes_alloc : ebytes;
-    ce = cudaHostRegister(g->edges, reg_bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
-    if (ce == cudaSuccess) e->registered = true;
-    else if (ce == cudaErrorHostMemoryAlreadyRegistered) cudaGetLastError();
-    else { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostRegister: %s", cudaGetErrorString(ce))); }
-    void *dp = nullptr;
-    ce = cudaHostGetDevicePointer(&dp, g->edges, 0);
-    if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce))); }
-    e->d_host_edges = (const uint32_t *)dp;
   }
-  // 16-byte host reads may run up to 12 bytes past the last record: allowed
-  // when the registered range is page-rounded (the library's allocations) or
-  // the record array is a whole number of 16-byte words.
-  {
-    const size_t rec_bytes = (size_t)e->m * 4 * e->W;
-    const bool rounded = e->h_packed != nullptr || g->owns || (rec_bytes % 16 == 0);
-    e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && e->d_host_edges &&
-                    ((uintptr_t)e->d_host_edges % 16 == 0) && rounded;
-  }
+  e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && e->d_host_edges &&
+                  ((uintptr_t)e->d_host_edges % 16 == 0);
   if (cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking) != cudaSuccess)
     return cleanup(fail(SGW_ECUDA, "stream creation"));
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < kMaxBuf; ++i) {
     if (cudaEventCreateWithFlags(&e->ev_ready[i], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&e->ev_free[i], cudaEventDisableTiming) != cudaSuccess)
       return cleanup(fail(SGW_ECUDA, "event creation"));
@@ -842,7 +1113,8 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   if (cudaEventCreate(&e->ev_t0) != cudaSuccess || cudaEventCreate(&e->ev_t1) != cudaSuccess)
     return cleanup(fail(SGW_ECUDA, "event creation"));
   if (cudaMallocHost(&e->h_ctl, sizeof(Ctl)) != cudaSuccess ||
-      cudaMallocHost(&e->h_parts, sizeof(Part) * (size_t)parts_host) != cudaSuccess)
+      cudaMallocHost(&e->h_parts, sizeof(Part) * (size_t)parts_host) != cudaSuccess ||
+      cudaMallocHost(&e->h_rstat, sizeof(RangeStat) * (size_t)parts_host) != cudaSuccess)
     return cleanup(fail(SGW_ECUDA, "pinned control block"));
   memset(e->h_ctl, 0, sizeof(Ctl));
   ce = cudaMemcpyAsync(e->d_off, g->node_pointer, 4ull * (e->n + 1), cudaMemcpyHostToDevice, e->s_comp);
@@ -861,19 +1133,18 @@ int sgw_engine_destroy(sgw_engine *e) {
   if (e->s_comp) cudaStreamSynchronize(e->s_comp);
   if (e->s_copy) cudaStreamSynchronize(e->s_copy);
   for (auto &pe : e->prof) { cudaEventDestroy(pe.a); cudaEventDestroy(pe.b); }
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < kMaxBuf; ++i) {
     if (e->ev_ready[i]) cudaEventDestroy(e->ev_ready[i]);
     if (e->ev_free[i]) cudaEventDestroy(e->ev_free[i]);
   }
+  if (e->h_rstat) cudaFreeHost(e->h_rstat);
   if (e->ev_t0) cudaEventDestroy(e->ev_t0);
   if (e->ev_t1) cudaEventDestroy(e->ev_t1);
   if (e->s_comp) cudaStreamDestroy(e->s_comp);
   if (e->s_copy) cudaStreamDestroy(e->s_copy);
   if (e->h_ctl) cudaFreeHost(e->h_ctl);
   if (e->h_parts) cudaFreeHost(e->h_parts);
-  if (e->registered) cudaHostUnregister(e->g->edges);
-  if (e->packed_registered) cudaHostUnregister(e->h_packed);
-  if (e->h_packed) host_free(e->h_packed);
+  if (e->h_packed) cudaFreeHost(e->h_packed);
   if (e->d_arena) cudaFree(e->d_arena);
   cudaGetLastError();
   delete e;
@@ -961,6 +1232,37 @@ int sgw_process_partition(sgw_engine *e, uint32_t i, uint32_t *inner_iterations)
   return SGW_OK;
 }
 
+int sgw_set_policy(sgw_engine *e, int policy, const sgw_mlp *model) {
+  clear_error();
+  if (!e) return fail(SGW_EINVAL, "null engine");
+  if (policy != SGW_POLICY_PLAIN && policy != SGW_POLICY_LEARNED)
+    return fail(SGW_EINVAL, "unknown policy %d", policy);
+  CK(cudaSetDevice(e->device));
+  if (model) {
+    if (mlp_device(model) != e->device) return fail(SGW_EINVAL, "model lives on another device");
+    CK(cudaMemcpy(e->d_mlp, mlp_device_weights(model), sizeof(__nv_bfloat16) * kMlpParams,
+                  cudaMemcpyDeviceToDevice));
+  }
+  e->have_model = model != nullptr;
+  e->policy = policy;
+  e->initialized = false;  // the step API restarts from sgw_state_init
+  return SGW_OK;
+}
+
+int sgw_range_trace_count(const sgw_engine *e, uint64_t *count) {
+  if (!e || !count) return fail(SGW_EINVAL, "null argument");
+  *count = e->rtrace.size();
+  return SGW_OK;
+}
+
+int sgw_range_trace_read(const sgw_engine *e, sgw_range_rec *out, uint64_t capacity, uint64_t *count) {
+  if (!e || !count) return fail(SGW_EINVAL, "null argument");
+  const uint64_t k = std::min<uint64_t>(capacity, e->rtrace.size());
+  if (out && k) memcpy(out, e->rtrace.data(), k * sizeof(sgw_range_rec));
+  *count = k;
+  return SGW_OK;
+}
+
 int sgw_trace_enable(sgw_engine *e, int on) {
   if (!e) return fail(SGW_EINVAL, "null engine");
   e->trace_on = on != 0;
@@ -1045,8 +1347,13 @@ int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values, sgw_run_st
     e->gitr = gitr;
     e->stats.active_vertices += e->num_active;
     e->stats.active_edges += e->num_active_edges;
-    TRY(process_iteration(e));
-    TRY(generate_and_plan(e, async ? 0 : 1));
+    if (e->policy == SGW_POLICY_LEARNED) {
+      TRY(process_iteration_ranges(e));
+      TRY(generate_and_stats(e, async ? 0 : 1));
+    } else {
+      TRY(process_iteration(e));
+      TRY(generate_and_plan(e, async ? 0 : 1));
+    }
   }
   CK(cudaEventRecord(e->ev_t1, e->s_comp));
   e->stats.global_iterations = gitr;

@@ -69,8 +69,7 @@ int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out) {
   return SGW_OK;
 }
 
-bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint32_t *nbits) {
-  *out = nullptr;
+bool pack_bits(const sgw_graph *g, uint32_t *nbits) {
   if (!g->weighted || g->m == 0) return false;
   uint32_t nb = 1;
   while (nb < 32 && (uint64_t(1) << nb) < g->n) ++nb;
@@ -80,10 +79,34 @@ bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint
 #pragma omp parallel for reduction(max : wmax)
   for (int64_t i = 0; i < (int64_t)g->m; ++i) wmax = std::max(wmax, ed[2 * size_t(i) + 1]);
   if ((uint64_t)wmax >= (uint64_t(1) << (32 - nb))) return false;
-  uint32_t *p = (uint32_t *)host_alloc(sizeof(uint32_t) * size_t(g->m), alloc_bytes);
-  if (!p) return false;
+  *nbits = nb;
+  return true;
+}
+
+void pack_into(const sgw_graph *g, uint32_t nb, uint32_t *p) {
+  const uint32_t *ed = (const uint32_t *)g->edges;
 #pragma omp parallel for
   for (int64_t i = 0; i < (int64_t)g->m; ++i) p[i] = (ed[2 * size_t(i) + 1] << nb) | ed[2 * size_t(i)];
+}
+
+void copy_records(const sgw_graph *g, void *out) {
+  const size_t total = size_t(g->m) * g->esz;
+  const size_t piece = size_t(64) << 20;
+  const int64_t pieces = (int64_t)((total + piece - 1) / piece);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < pieces; ++k) {
+    const size_t a = size_t(k) * piece, b = std::min(total, a + piece);
+    memcpy((char *)out + a, (const char *)g->edges + a, b - a);
+  }
+}
+
+bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint32_t *nbits) {
+  *out = nullptr;
+  uint32_t nb = 0;
+  if (!pack_bits(g, &nb)) return false;
+  uint32_t *p = (uint32_t *)host_alloc(sizeof(uint32_t) * size_t(g->m), alloc_bytes);
+  if (!p) return false;
+  pack_into(g, nb, p);
   *out = p;
   *nbits = nb;
   return true;

@@ -36,6 +36,15 @@ int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out);
 // with nbits = bits of the largest vertex id.  Returns false, allocating
 // nothing, when some weight does not fit in the remaining 32 - nbits bits.
 bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint32_t *nbits);
+// The same decision and fill into a caller-provided array of m words.
+bool pack_bits(const sgw_graph *g, uint32_t *nbits);
+void pack_into(const sgw_graph *g, uint32_t nbits, uint32_t *out);
+// Parallel copy of the edge records (m * esz bytes) into out.
+void copy_records(const sgw_graph *g, void *out);
+
+// Device address of a scheduler model's BF16 weights, and its device.
+const void *mlp_device_weights(const sgw_mlp *m);
+int mlp_device(const sgw_mlp *m);
 
 // Greedy partition planner shared by the host entry point and the device
 // planner: largest prefix of the queue starting at `from` whose edge count

@@ -18,6 +18,7 @@
 #include <stdint.h>
 
 #include "sgw_internal.h"
+#include "sgw_mlp.cuh"
 
 namespace sgw {
 
@@ -35,6 +36,8 @@ struct Ctl {
   uint32_t upd[4];           // async inner iteration k: relaxations that improved
   uint32_t wl_count[4];      // chunk-list items of inner iteration k
   uint32_t iters_run;        // inner iterations that did work
+  uint32_t dq_count[4];      // async: partition sources dirtied in inner iteration k
+  uint32_t dq_overflow[4];   //   and whether that list overflowed (then: full scan)
   uint32_t hub_active;       // single-vertex partition: the source was dirty
   uint32_t hub_value;        // single-vertex partition: its value
   uint32_t pad0;
@@ -50,6 +53,8 @@ struct Part {                // one partition of the active queue
   uint32_t edge_from;        // ptr[from]
   uint32_t first_vertex;     // queue[from]
   unsigned long long edge_count;
+  uint32_t last_vertex;      // queue[from + size - 1]
+  uint32_t pad;
 };
 
 struct WorkItem {            // a chunk of one high-degree source's edges
@@ -80,6 +85,16 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
+}
+
+// First index in a[0, n) whose value is >= x (a sorted ascending).
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t n, uint32_t x) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
 }
 
 // Warp-inclusive scan of a u32.
@@ -305,6 +320,8 @@ __global__ void k_plan(const uint32_t *ptr, const uint32_t *queue, Ctl *ctl,
       q.size = to - from;
       q.edge_from = ptr[from];
       q.first_vertex = queue[from];
+      q.last_vertex = queue[to - 1];
+      q.pad = 0;
       q.edge_count = (unsigned long long)ptr[to] - ptr[from];
       parts[p] = q;
     }
@@ -543,16 +560,42 @@ template <> struct Op<SGW_CC> {    // cc_kernel: value, atomicMin (:96-98)
   __device__ static uint32_t cand(uint32_t v, uint32_t) { return v; }
 };
 
+// Async inner iterations after the first only need the partition sources
+// that the previous iteration dirtied.  The thread whose atomicOr first sets
+// a destination's label appends it here when its id lies in the partition's
+// id range; the next iteration relaxes the listed vertices that are queued in
+// the partition (binary search in the sorted queue) instead of scanning every
+// partition source.  On overflow the next iteration scans as before.
+struct DirtyList {
+  uint32_t *out;
+  uint32_t *count;
+  uint32_t *overflow;
+  uint32_t cap;
+  uint32_t lo, hi;
+};
+
 // Relaxes one edge; returns true if the destination improved.
-template <int ALGO>
+template <int ALGO, bool DL = false>
 __device__ __forceinline__ bool relax_edge(uint32_t sval, uint32_t dst, uint32_t w,
-                                           uint32_t *value, uint8_t *nxt) {
+                                           uint32_t *value, uint8_t *nxt, const DirtyList *dl = nullptr) {
   const uint32_t c = Op<ALGO>::cand(sval, w);
   const uint32_t cur = value[dst];
   if (Op<ALGO>::kMax ? (c > cur) : (c < cur)) {
     const uint32_t old = Op<ALGO>::kMax ? atomicMax(&value[dst], c) : atomicMin(&value[dst], c);
     if (Op<ALGO>::kMax ? (c > old) : (c < old)) {
-      nxt[dst] = 1;
+      if (DL) {
+        // label arrays are 256-byte aligned: set the byte through its word
+        uint32_t *word = reinterpret_cast<uint32_t *>(nxt + (dst & ~3u));
+        const uint32_t sh = 8u * (dst & 3u);
+        const uint32_t prev = atomicOr(word, 1u << sh);
+        if (((prev >> sh) & 0xffu) == 0 && dst >= dl->lo && dst <= dl->hi) {
+          const uint32_t slot = atomicAdd(dl->count, 1u);
+          if (slot < dl->cap) dl->out[slot] = dst;
+          else *dl->overflow = 1u;
+        }
+      } else {
+        nxt[dst] = 1;
+      }
       return true;
     }
   }
@@ -600,9 +643,31 @@ struct RelaxArgs {
   uint32_t tile_degree_max;  // sources above this go to the chunk list
   uint32_t chunk_edges;
   uint32_t pbits;            // packed records: bits of the destination
+  // streamed partition: the buffer holds a whole vertex range starting at
+  // edge stream_base, so a source's edges sit at off[u] - stream_base
+  uint32_t streamed;
+  uint32_t stream_base;
+  const uint32_t *off;
+  // async dirty lists (iteration k writes dq_out, iteration k + 1 reads it)
+  const uint32_t *dq_in;
+  uint32_t *dq_out;
+  uint32_t dq_cap;
+  uint32_t v_lo, v_hi;       // vertex ids of the partition's first and last source
 };
 
 constexpr int kRelaxThreads = 256;
+
+template <bool ASYNC>
+__device__ __forceinline__ DirtyList make_dirty_list(const RelaxArgs &a) {
+  DirtyList dl;
+  dl.out = a.dq_out;
+  dl.count = &a.ctl->dq_count[a.iter & 3u];
+  dl.overflow = &a.ctl->dq_overflow[a.iter & 3u];
+  dl.cap = a.dq_cap;
+  dl.lo = a.v_lo;
+  dl.hi = a.v_hi;
+  return dl;
+}
 
 // Tile of kRelaxThreads partition sources per CTA (grid-stride).  Each thread
 // claims one source (async: only if its label is set, clearing it), the CTA
@@ -618,28 +683,55 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
   __shared__ uint32_t s_hub[kRelaxThreads];
   __shared__ uint32_t s_nhub, s_wbase;
   __shared__ int s_skip;
+  __shared__ uint32_t s_nsrc;
   const int tid = threadIdx.x;
   const uint32_t slot = a.iter & 3u;
+  // async iterations after the first read the previous iteration's dirty list
+  const bool listed = ASYNC && a.iter > 1 && a.dq_in != nullptr;
   if (tid == 0) {
     int skip = 0;
     if (ASYNC && a.iter > 1 && ld_acquire_u32(&a.ctl->upd[(a.iter - 1) & 3u]) == 0) skip = 1;
     s_skip = skip;
+    uint32_t nsrc = a.size;
+    if (listed) {
+      const uint32_t prev = (a.iter - 1) & 3u;
+      if (ld_acquire_u32(&a.ctl->dq_overflow[prev]) == 0)
+        nsrc = min(ld_acquire_u32(&a.ctl->dq_count[prev]), a.dq_cap);
+      else
+        nsrc = 0xffffffffu;  // overflowed: scan the partition
+    }
+    s_nsrc = nsrc;
     if (blockIdx.x == 0) {
       a.ctl->upd[(a.iter + 1) & 3u] = 0;
       a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
+      a.ctl->dq_count[(a.iter + 1) & 3u] = 0;
+      a.ctl->dq_overflow[(a.iter + 1) & 3u] = 0;
       if (!skip) atomicAdd(&a.ctl->iters_run, 1u);
     }
   }
   __syncthreads();
   if (s_skip) return;
+  const bool from_list = listed && s_nsrc != 0xffffffffu;
+  const uint32_t nsrc = from_list ? s_nsrc : a.size;
+  const DirtyList dl = make_dirty_list<ASYNC>(a);
   bool any_update = false;
-  const uint32_t ntiles = (a.size + kRelaxThreads - 1) / kRelaxThreads;
+  const uint32_t ntiles = (nsrc + kRelaxThreads - 1) / kRelaxThreads;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     if (tid == 0) s_nhub = 0;
     __syncthreads();
-    const uint32_t i = a.from + t * kRelaxThreads + tid;
+    const uint32_t idx = t * kRelaxThreads + tid;
+    uint32_t i = 0xffffffffu;
+    if (idx < nsrc) {
+      if (from_list) {  // a dirtied vertex: is it queued in this partition?
+        const uint32_t v = a.dq_in[idx];
+        const uint32_t pos = lower_bound_u32(a.queue + a.from, a.size, v);
+        if (pos < a.size && a.queue[a.from + pos] == v) i = a.from + pos;
+      } else {
+        i = a.from + idx;
+      }
+    }
     uint32_t d = 0, boff = 0, val = 0, u = 0;
-    if (i < a.from + a.size) {
+    if (i != 0xffffffffu) {
       u = a.queue[i];
       bool act = true;
       if (ASYNC) {
@@ -651,7 +743,7 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
         if (can_push<ALGO>(val)) {
           const uint32_t p0 = a.ptr[i];
           d = a.ptr[i + 1] - p0;
-          boff = p0 - a.edge_from;
+          boff = a.streamed ? a.off[u] - a.stream_base : p0 - a.edge_from;
           if (d > a.tile_degree_max) {
             s_hub[atomicAdd(&s_nhub, 1u)] = tid;
             atomicAdd(&a.ctl->relaxed_edges, (unsigned long long)d);
@@ -723,7 +815,7 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
       const uint32_t e = s_boff[k] + (j - s_scan[k]);
       uint32_t dst, w;
       load_edge<W>(a.buf, e, a.pbits, dst, w);
-      any_update |= relax_edge<ALGO>(s_val[k], dst, w, a.value, a.nxt);
+      any_update |= relax_edge<ALGO, ASYNC>(s_val[k], dst, w, a.value, a.nxt, &dl);
     }
     __syncthreads();
   }
@@ -739,13 +831,14 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_chunks(RelaxArgs a) {
   const int lane = threadIdx.x & 31;
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  const DirtyList dl = make_dirty_list<ASYNC>(a);
   bool any_update = false;
   for (uint32_t it = gw; it < items; it += nw) {
     const WorkItem wi = a.wl[it];
     for (uint32_t j = lane; j < wi.count; j += 32) {
       uint32_t dst, w;
       load_edge<W>(a.buf, wi.boff + j, a.pbits, dst, w);
-      any_update |= relax_edge<ALGO>(wi.value, dst, w, a.value, a.nxt);
+      any_update |= relax_edge<ALGO, ASYNC>(wi.value, dst, w, a.value, a.nxt, &dl);
     }
   }
   if (__syncthreads_or(any_update) && threadIdx.x == 0) atomicAdd(&a.ctl->upd[slot], 1u);
@@ -862,6 +955,9 @@ struct PrArgs {
   uint32_t tile_degree_max;
   uint32_t chunk_edges;
   uint32_t pbits;
+  uint32_t streamed;
+  uint32_t stream_base;
+  const uint32_t *off;
   double acc;
   double damping;
 };
@@ -927,7 +1023,7 @@ __global__ void __launch_bounds__(kRelaxThreads) k_pr_tile(PrArgs a) {
       if (act) {
         any_push = true;
         d = deg;
-        boff = p0 - a.edge_from;
+        boff = a.streamed ? a.off[a.queue[i]] - a.stream_base : p0 - a.edge_from;
         if (d > a.tile_degree_max) {
           s_hub[atomicAdd(&s_nhub, 1u)] = tid;
           atomicAdd(&a.ctl->relaxed_edges, (unsigned long long)d);
@@ -1036,6 +1132,70 @@ __global__ void k_pr_init(uint32_t n, double init, double *pval, double *delta) 
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     pval[v] = 0.0;
     delta[v] = init;
+  }
+}
+
+// ---- learned scheduler: per-range statistics and prediction -------------------
+struct RangeInfo {           // a static vertex range [v0, v1) with edges [e0, e1)
+  uint32_t v0, v1, e0, e1;
+};
+
+struct RangeStat {           // one global iteration of one range
+  uint32_t qa, qb;           // its segment of the active queue
+  uint32_t edge_from;        // ptr[qa]
+  uint32_t act_edges;        // ptr[qb] - ptr[qa]
+  uint32_t prev_edges;       // act_edges of the previous global iteration
+  uint32_t first_vertex;     // queue[qa]
+  float pred;                // predicted active edge fraction next iteration
+  float feat[kMlpIn];
+  uint32_t pad;
+  uint32_t last_vertex;      // queue[qb - 1]
+};
+
+// One warp per range: locate the range's queue segment, form the five
+// features, evaluate the network (or, with no weights, predict that the
+// current active edge fraction persists).
+__global__ void k_range_stats(const RangeInfo *__restrict__ ranges, uint32_t num_ranges,
+                              const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
+                              const Ctl *__restrict__ ctl, RangeStat *st,
+                              const __nv_bfloat16 *__restrict__ w, uint32_t iter, uint32_t cap) {
+  const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (s >= num_ranges) return;
+  const RangeInfo r = ranges[s];
+  const uint32_t count = ctl->num_active;
+  uint32_t qa = 0, qb = 0;
+  if (lane == 0) {
+    qa = lower_bound_u32(queue, count, r.v0);
+    qb = qa + lower_bound_u32(queue + qa, count - qa, r.v1);
+  }
+  qa = __shfl_sync(0xffffffffu, qa, 0);
+  qb = __shfl_sync(0xffffffffu, qb, 0);
+  const uint32_t efrom = ptr[qa];
+  const uint32_t act = ptr[qb] - efrom;
+  const uint32_t prev = st[s].prev_edges;
+  const float redges = (float)(r.e1 - r.e0);
+  float x[kMlpIn];
+  x[0] = (r.v1 > r.v0) ? (float)(qb - qa) / (float)(r.v1 - r.v0) : 0.0f;
+  x[1] = redges > 0.0f ? (float)act / redges : 0.0f;
+  x[2] = fminf(fmaxf(__log2f(((float)act + 1.0f) / ((float)prev + 1.0f)) / 16.0f, -1.0f), 1.0f);
+  x[3] = fminf((float)iter, 64.0f) / 64.0f;
+  x[4] = cap ? fminf(redges / (float)cap, 1.0f) : 0.0f;
+  const float pred = w ? mlp_forward_warp(w, x, lane) : x[1];
+  if (lane == 0) {
+    RangeStat o;
+    o.qa = qa;
+    o.qb = qb;
+    o.edge_from = efrom;
+    o.act_edges = act;
+    o.prev_edges = act;  // becomes "previous" for the next iteration
+    o.first_vertex = qb > qa ? queue[qa] : r.v0;
+    o.last_vertex = qb > qa ? queue[qb - 1] : r.v0;
+    o.pred = pred;
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) o.feat[k] = x[k];
+    o.pad = prev;        // the previous count, reported with this iteration
+    st[s] = o;
   }
 }
 

@@ -29,7 +29,8 @@ MODES = {"sync": SYNC, "async": ASYNC}
 class EngineOpts(C.Structure):
     _fields_ = [("budget_bytes", C.c_uint64), ("device", C.c_int32), ("flags", C.c_uint32),
                 ("inner_batch", C.c_uint32), ("tile_degree_max", C.c_uint32),
-                ("chunk_edges", C.c_uint32), ("gather_ctas", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+                ("chunk_edges", C.c_uint32), ("gather_ctas", C.c_uint32), ("num_buffers", C.c_uint32),
+                ("reserved", C.c_uint32 * 6)]
 
 
 class RunParams(C.Structure):
@@ -89,6 +90,23 @@ _PROTOS = {
     "sgw_device_count": (C.c_int, [C.POINTER(C.c_int)]),
     "sgw_probe_link": (C.c_int, [C.c_int, C.c_uint64, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "sgw_generate_noalloc": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_int, _P, _P, _P, _u32p, _u64p]),
+    "sgw_mlp_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_P)]),
+    "sgw_mlp_destroy": (C.c_int, [_P]),
+    "sgw_mlp_set_params": (C.c_int, [_P, _P]),
+    "sgw_mlp_get_params": (C.c_int, [_P, _P]),
+    "sgw_mlp_forward": (C.c_int, [_P, _P, C.c_uint32, _P]),
+    "sgw_mlp_gradient": (C.c_int, [_P, _P, _P, C.c_uint32, _P, C.POINTER(C.c_float)]),
+    "sgw_mlp_train": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint32, C.c_float, C.POINTER(C.c_float)]),
+    "sgw_mlp_save": (C.c_int, [_P, C.c_char_p]),
+    "sgw_mlp_load": (C.c_int, [C.c_int, C.c_char_p, C.POINTER(_P)]),
+    "sgw_set_policy": (C.c_int, [_P, C.c_int, _P]),
+    "sgw_batch_create": (C.c_int, [_P, C.POINTER(EngineOpts), C.c_uint32, C.POINTER(_P)]),
+    "sgw_batch_destroy": (C.c_int, [_P]),
+    "sgw_batch_device_bytes": (C.c_int, [_P, _u64p]),
+    "sgw_batch_run": (C.c_int, [_P, C.c_int, _P, C.c_uint32, _P, _P]),
+    "sgw_batch_results": (C.c_int, [_P, C.POINTER(_P)]),
+    "sgw_range_trace_count": (C.c_int, [_P, _u64p]),
+    "sgw_range_trace_read": (C.c_int, [_P, _P, C.c_uint64, _u64p]),
     "sgw_trace_enable": (C.c_int, [_P, C.c_int]),
     "sgw_trace_count": (C.c_int, [_P, _u64p]),
     "sgw_trace_read": (C.c_int, [_P, _P, C.c_uint64, _u64p]),
@@ -358,3 +376,157 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+# ---- learned scheduler ------------------------------------------------------------
+POLICY_PLAIN, POLICY_LEARNED = 0, 1
+MLP_INPUTS, MLP_PARAMS = 5, 4609
+ACT_SKIP, ACT_RESIDENT, ACT_STREAM, ACT_COMPACT, ACT_SPLIT = 0, 1, 2, 3, 4
+
+RANGE_REC = np.dtype([("global_iteration", "<u4"), ("range", "<u4"), ("active_nodes", "<u4"),
+                      ("range_nodes", "<u4"), ("active_edges", "<u4"), ("range_edges", "<u4"),
+                      ("action", "<u4"), ("inner_iterations", "<u4"), ("features", "<f4", (5,)),
+                      ("predicted", "<f4"), ("bytes_h2d", "<u8")])
+
+
+class Mlp:
+    """The scheduler's network (BF16 weights on the device)."""
+
+    def __init__(self, handle: int):
+        self.h = C.c_void_p(handle)
+
+    @classmethod
+    def create(cls, device=0, seed=1):
+        h = _P()
+        check(lib().sgw_mlp_create(device, seed, C.byref(h)), "sgw_mlp_create")
+        return cls(h.value)
+
+    @classmethod
+    def load(cls, path, device=0):
+        h = _P()
+        check(lib().sgw_mlp_load(device, str(path).encode(), C.byref(h)), f"sgw_mlp_load({path})")
+        return cls(h.value)
+
+    def save(self, path):
+        check(lib().sgw_mlp_save(self.h, str(path).encode()), f"sgw_mlp_save({path})")
+
+    def params(self) -> np.ndarray:
+        out = np.empty(MLP_PARAMS, np.float32)
+        check(lib().sgw_mlp_get_params(self.h, _ptr(out)), "sgw_mlp_get_params")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (MLP_PARAMS,)
+        check(lib().sgw_mlp_set_params(self.h, _ptr(p)), "sgw_mlp_set_params")
+
+    def forward(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_INPUTS)
+        y = np.empty(len(x), np.float32)
+        check(lib().sgw_mlp_forward(self.h, _ptr(x), len(x), _ptr(y)), "sgw_mlp_forward")
+        return y
+
+    def gradient(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_INPUTS)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.empty(MLP_PARAMS, np.float32)
+        loss = C.c_float()
+        check(lib().sgw_mlp_gradient(self.h, _ptr(x), _ptr(t), len(x), _ptr(g), C.byref(loss)),
+              "sgw_mlp_gradient")
+        return g, loss.value
+
+    def train(self, x, t, steps=500, lr=3e-3) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_INPUTS)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = C.c_float()
+        check(lib().sgw_mlp_train(self.h, _ptr(x), _ptr(t), len(x), steps, lr, C.byref(loss)), "sgw_mlp_train")
+        return loss.value
+
+    def close(self):
+        if self.h and self.h.value:
+            lib().sgw_mlp_destroy(self.h)
+            self.h = C.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _engine_set_policy(self, policy, model: "Mlp | None" = None):
+    p = {"plain": POLICY_PLAIN, "learned": POLICY_LEARNED}.get(policy, policy)
+    check(lib().sgw_set_policy(self.h, p, model.h if model is not None else None), "sgw_set_policy")
+
+
+def _engine_trace_enable(self, on=True):
+    check(lib().sgw_trace_enable(self.h, int(on)), "sgw_trace_enable")
+
+
+def _engine_range_trace(self) -> np.ndarray:
+    cnt = C.c_uint64()
+    check(lib().sgw_range_trace_count(self.h, C.byref(cnt)), "sgw_range_trace_count")
+    out = np.zeros(cnt.value, RANGE_REC)
+    got = C.c_uint64()
+    check(lib().sgw_range_trace_read(self.h, out.ctypes.data if cnt.value else None, cnt.value, C.byref(got)),
+          "sgw_range_trace_read")
+    return out[: got.value]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("queries", C.c_uint32), ("ms_device", C.c_double),
+                ("ms_wall", C.c_double), ("d2h_bytes", C.c_uint64), ("reserved", C.c_uint64 * 4)]
+
+
+class Batch:
+    """Up to 64 BFS/SSSP queries per traversal over a graph held in HBM."""
+
+    def __init__(self, graph: Graph, lanes=64, budget_bytes=0, device=0, chunk_edges=0, flags=0):
+        o = default_opts()
+        o.budget_bytes = int(budget_bytes)
+        o.device = device
+        o.flags = flags
+        o.chunk_edges = chunk_edges
+        h = _P()
+        check(lib().sgw_batch_create(graph.h, C.byref(o), lanes, C.byref(h)), "sgw_batch_create")
+        self.h = C.c_void_p(h.value)
+        self.graph = graph
+        self.lanes = lanes
+
+    def run(self, algo, sources, out=None, view=False):
+        """Distances of each query (rows).  view=True returns a read-only view of
+        the batch's pinned buffer (no copy; valid until the next run)."""
+        src = np.ascontiguousarray(sources, dtype=np.uint32)
+        n = self.graph.n
+        if out is None and not view:
+            out = np.empty((len(src), n), np.uint32)
+        st = BatchStats()
+        check(lib().sgw_batch_run(self.h, ALGOS.get(algo, algo), _ptr(src), len(src),
+                                  _ptr(out) if out is not None else None, C.byref(st)), "sgw_batch_run")
+        if out is None:
+            p = _P()
+            check(lib().sgw_batch_results(self.h, C.byref(p)), "sgw_batch_results")
+            out = np.ctypeslib.as_array(C.cast(p, _u32p), shape=(len(src), n))
+            out.flags.writeable = False
+        return out, {k: getattr(st, k) for k, _ in st._fields_ if k != "reserved"}
+
+    def device_bytes(self) -> int:
+        v = C.c_uint64()
+        check(lib().sgw_batch_device_bytes(self.h, C.byref(v)), "sgw_batch_device_bytes")
+        return v.value
+
+    def close(self):
+        if self.h and self.h.value:
+            lib().sgw_batch_destroy(self.h)
+            self.h = C.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+Engine.set_policy = _engine_set_policy
+Engine.trace_enable = _engine_trace_enable
+Engine.range_trace = _engine_range_trace
