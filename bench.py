@@ -68,6 +68,10 @@ def parse_args():
                     help="both: time the plain (reference) schedule, then the learned one (headline)")
     ap.add_argument("--model", default="", help="scheduler model file; 'none' = persistence predictor")
     ap.add_argument("--num-buffers", type=int, default=3, help="edge buffers of the learned policy")
+    ap.add_argument("--sched-inner", type=int, default=0,
+                    help="learned policy: inner-iteration cap of kept ranges predicted active (0 = library default)")
+    ap.add_argument("--sched-permille", type=int, default=0,
+                    help="learned policy: predicted active fraction (1/1000) that caps a kept range (0 = default)")
     return ap.parse_args()
 
 
@@ -211,7 +215,8 @@ def run_ours(a, dist):
         nb = a.num_buffers if policy == "learned" else 0
         e = N.Engine(g, budget_bytes=int(a.budget), device=dev, flags=flags, gather_ctas=a.gather_ctas,
                      tile_degree_max=a.tile_degree_max, chunk_edges=a.chunk_edges,
-                     inner_batch=a.inner_batch, num_buffers=nb)
+                     inner_batch=a.inner_batch, num_buffers=nb, sched_inner=a.sched_inner,
+                     sched_active_permille=a.sched_permille)
         if policy == "learned":
             from subway_gb300 import scheduler
             model = None if a.model == "none" else (N.Mlp.load(a.model, dev) if a.model else
@@ -248,9 +253,17 @@ def run_ours(a, dist):
                              "ms_per_step": round(sum(s["ms_device"] for s in steps) / a.steps, 4),
                              "iterations_per_step": round(sum(s["global_iterations"] for s in steps) / a.steps, 2)}
             eng.close()
+    mispredicted = None
     if a.policy in ("learned", "both"):
         eng = engine("learned")
         steps, clk, t_total = measure(eng)
+        # one more run, untimed, with the range trace on: how often the
+        # predictions behind its transfer decisions were wrong
+        from subway_gb300 import scheduler
+        eng.trace_enable(True)
+        eng.run(a.algo, a.mode, int(sources[0]), out=out)
+        mispredicted = scheduler.mispredictions(eng.range_trace())
+        eng.trace_enable(False)
     reached = sum(s["reached_edges"] for s in steps)
     dev_ms = sum(s["ms_device"] for s in steps)
     wall_ms = sum(s["wall_ms"] for s in steps)
@@ -269,7 +282,7 @@ def run_ours(a, dist):
     launches = {"gather": sum(s["gather_launches"] for s in steps),
                 "relax": sum(s["relax_launches"] for s in steps),
                 "generate": sum(s["generate_launches"] for s in steps)}
-    esz = 8 if weighted else 4
+    esz = 8 if weighted and a.no_pack else 4  # device edge record (packed when weighted)
     relax_bytes = sum(s["relaxed_sources"] * 17 + s["relaxed_edges"] * (esz + 4) for s in steps)
     gen_bytes = sum(s["generate_launches"] * 2 * g.n + s["active_vertices"] * 16 for s in steps)
     hbm_peak, hbm_src = measured_peaks()
@@ -291,10 +304,8 @@ def run_ours(a, dist):
                       "ms_per_launch": round(kv["ms"] / max(launches[name], 1), 4),
                       "bytes_per_launch": round(kv["bytes"] / max(launches[name], 1)),
                       "peak_source": kv["peak_src"]}
-    traffic = load_traffic()
     for name in roof:
-        if name in traffic:
-            roof[name]["traffic"] = traffic[name]
+        roof[name]["traffic"] = traffic_per_launch(name, roof[name]["bytes_per_launch"])
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "GTEPS", "n_gpus": dist.world, "steps": K,
         "warmup": a.warmup, "ms_per_step": round(dev_ms_max / K, 4), "higher_is_better": True,
@@ -307,7 +318,8 @@ def run_ours(a, dist):
         "learned_over_plain": (None if not plain_summary else
                                {"speedup": round(value / plain_summary["value"], 3),
                                 "e2e_speedup": round(e2e / plain_summary["e2e"], 3),
-                                "h2d_bytes_ratio": round(h2d / max(plain_summary["h2d_bytes_per_run"], 1), 3)}),
+                                "h2d_bytes_ratio": round(h2d / max(plain_summary["h2d_bytes_per_run"], 1), 3),
+                                "mispredictions": mispredicted}),
         "e2e": {"value": round(e2e, 4), "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(wall_ms_max / K, 4)},
         "h2d_bytes_per_run": int(h2d),
@@ -332,15 +344,16 @@ def probe_link(N, dev):
     return h.value, d.value
 
 
-def load_traffic():
-    """Per-launch DRAM bytes from the committed ncu summary, if present."""
-    p = ROOT / "profiles" / "traffic.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text())
-        except ValueError:
-            return {}
-    return {}
+# DRAM bytes (read + write) per algorithmic byte, from one ncu capture of
+# each kernel on a small case (profiles/k_gather_v_rmat21.md, launch 3;
+# profiles/k_relax_tile_rmat21.md; profiles/k_generate_rmat21.md); a full-size
+# launch's traffic is this ratio times its algorithmic bytes.
+DRAM_PER_ALGO_BYTE = {"gather": 1.21}
+
+
+def traffic_per_launch(name, bytes_per_launch):
+    r = DRAM_PER_ALGO_BYTE.get(name)
+    return None if r is None else int(r * bytes_per_launch)
 
 
 def run_reference(a, dist):

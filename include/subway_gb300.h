@@ -98,6 +98,8 @@ void sgw_graph_free(sgw_graph *g);
 #define SGW_OPT_NO_PACK    0x4u
 /* Gather host records one per thread instead of as aligned 16-byte words. */
 #define SGW_OPT_SCALAR_GATHER 0x8u
+/* sched_flags: the learned policy's inner cap also covers compacted ranges */
+#define SGW_SCHED_CAP_COMPACT 0x1u
 
 typedef struct sgw_engine_opts {
   /* Device-memory budget in bytes for everything the engine allocates.
@@ -112,7 +114,19 @@ typedef struct sgw_engine_opts {
   uint32_t gather_ctas;    /* CTAs of the gather kernel, 0 = 2 per SM          */
   uint32_t num_buffers;    /* device edge buffers sharing the budget, 0 = 2
                               (1 with SGW_OPT_NO_OVERLAP), at most 8          */
-  uint32_t reserved[6];
+  /* Learned policy, async mode: a range whose predicted active-edge fraction
+   * for the next global iteration is at least sched_active_permille / 1000
+   * (0 = 1) runs at most sched_inner inner iterations (0 = 2) now, since what
+   * further passes would settle is likely to be redone when it is relaxed
+   * again; other ranges run to local convergence.  Without
+   * SGW_SCHED_CAP_COMPACT the cap only covers ranges that stay in their edge
+   * buffer (their leftover sources cost no transfer).
+   * sched_active_permille > 1000 turns the cap off.  Defaults: 2, 1,
+   * SGW_SCHED_CAP_COMPACT. */
+  uint32_t sched_inner;
+  uint32_t sched_active_permille;
+  uint32_t sched_flags;    /* SGW_SCHED_*                                     */
+  uint32_t reserved[3];
 } sgw_engine_opts;
 
 void sgw_engine_opts_default(sgw_engine_opts *opts);

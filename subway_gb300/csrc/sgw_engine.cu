@@ -60,8 +60,7 @@ struct sgw_engine {
   uint32_t *d_off = nullptr;
   uint32_t *d_value = nullptr;
   uint8_t *d_l1 = nullptr, *d_l2 = nullptr;
-  uint32_t *d_dq[2] = {nullptr, nullptr};  // async dirty lists (ping-pong)
-  uint32_t dq_cap = 0;
+  uint32_t range_inner_cap = 0;  // learned policy: inner-iteration cap of the running range
   uint32_t *d_queue = nullptr, *d_ptr = nullptr;
   uint32_t *d_tflag = nullptr;
   unsigned long long *d_tagg = nullptr, *d_tincl = nullptr;
@@ -188,8 +187,7 @@ enum Family { FAM_INT = 0, FAM_PR = 1 };
 struct Layout {
   size_t off, tflag, tagg, tincl, ctl, mlp;           // common
   size_t value, l1, l2, queue, ptr, delta, qpush;     // family
-  size_t parts, ranges, rstat, wl, dq0, dq1, buf[kMaxBuf], total;
-  uint32_t dq_cap;
+  size_t parts, ranges, rstat, wl, buf[kMaxBuf], total;
   uint64_t cap;
   uint32_t max_parts, wl_cap;
 };
@@ -216,10 +214,6 @@ Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
   L.queue = take(4ull * n);
   L.ptr = take(4ull * (n + 1));
   if (fam == FAM_PR) L.qpush = take(8ull * n);
-  // async dirty lists: n / 8 entries each (overflow falls back to a scan)
-  L.dq_cap = fam == FAM_INT ? std::max<uint32_t>(4096u, n / 8) : 0u;
-  L.dq0 = take(4ull * L.dq_cap);
-  L.dq1 = take(4ull * L.dq_cap);
   L.cap = cap;
   L.max_parts = (uint32_t)std::min<uint64_t>(2ull * ((uint64_t)m / std::max<uint64_t>(cap, 1) + 1) + 2,
                                              0x7fffffffull);
@@ -271,9 +265,6 @@ int carve(sgw_engine *e, int fam, uint64_t cap) {
   e->d_value = (uint32_t *)(b + L.value);
   e->d_l1 = fam == FAM_INT ? (uint8_t *)(b + L.l1) : nullptr;
   e->d_l2 = fam == FAM_INT ? (uint8_t *)(b + L.l2) : nullptr;
-  e->d_dq[0] = L.dq_cap ? (uint32_t *)(b + L.dq0) : nullptr;
-  e->d_dq[1] = L.dq_cap ? (uint32_t *)(b + L.dq1) : nullptr;
-  e->dq_cap = L.dq_cap;
   e->d_pval = fam == FAM_PR ? (double *)(b + L.value) : nullptr;
   e->d_delta = fam == FAM_PR ? (double *)(b + L.delta) : nullptr;
   e->d_qpush = fam == FAM_PR ? (double *)(b + L.qpush) : nullptr;
@@ -478,11 +469,6 @@ int launch_relax_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, u
   a.streamed = e->cur_streamed;
   a.stream_base = e->cur_stream_base;
   a.off = e->d_off;
-  a.dq_in = (ASYNC && iter > 1) ? e->d_dq[(iter - 1) & 1u] : nullptr;
-  a.dq_out = e->d_dq[iter & 1u];
-  a.dq_cap = e->dq_cap;
-  a.v_lo = q.first_vertex;
-  a.v_hi = q.last_vertex;
   const uint32_t g1 = grid_for(e, q.size, kRelaxThreads);
   k_relax_tile<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
   CK(cudaGetLastError());
@@ -615,8 +601,8 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
 // then inner iterations until no relaxation improves (or max_inner).
 int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_out) {
   const bool async = e->params.mode == SGW_ASYNC;
-  // upd, wl_count, iters_run, dq_count, dq_overflow
-  CK(cudaMemsetAsync(&e->d_ctl->upd[0], 0, sizeof(uint32_t) * 17, e->s_comp));
+  // upd, wl_count, iters_run
+  CK(cudaMemsetAsync(&e->d_ctl->upd[0], 0, sizeof(uint32_t) * 9, e->s_comp));
   if (!async) {
     size_t slot = 0;
     TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
@@ -631,7 +617,8 @@ int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_o
     CK(cudaGetLastError());
     e->stats.launches += 1;
   }
-  const uint32_t max_inner = e->params.max_inner ? e->params.max_inner : 0xffffffffu;
+  uint32_t max_inner = e->params.max_inner ? e->params.max_inner : 0xffffffffu;
+  if (e->range_inner_cap) max_inner = std::min(max_inner, e->range_inner_cap);
   uint32_t iter = 1;
   const uint32_t batch = std::max<uint32_t>(1, e->opts.inner_batch);
   while (true) {
@@ -753,8 +740,10 @@ int generate_and_stats(sgw_engine *e, int consume) {
 }
 
 struct Job {
-  uint32_t s;       // range
+  uint32_t s;       // first range
+  uint32_t s_end;   // one past the last range (consecutive compacted ranges merge)
   uint32_t action;  // SGW_ACT_*
+  Part part;        // the queue segment relaxed
   int buf = -1;     // buffer it is processed from
   bool ready = false;
 };
@@ -765,8 +754,6 @@ Part range_part(const RangeStat &st) {
   q.size = st.qb - st.qa;
   q.edge_from = st.edge_from;
   q.first_vertex = st.first_vertex;
-  q.last_vertex = st.last_vertex;
-  q.pad = 0;
   q.edge_count = st.act_edges;
   return q;
 }
@@ -774,7 +761,6 @@ Part range_part(const RangeStat &st) {
 // Enqueues job j's transfer into buffer b on the copy stream.
 int range_transfer(sgw_engine *e, Job &j, int b) {
   const RangeInfo &r = e->ranges[j.s];
-  const RangeStat &st = e->h_rstat[j.s];
   if (j.action == SGW_ACT_STREAM) {
     const size_t esz = 4ull * e->W;
     const size_t bytes = (size_t)(r.e1 - r.e0) * esz;
@@ -790,7 +776,7 @@ int range_transfer(sgw_engine *e, Job &j, int b) {
     e->stats.h2d_bytes += bytes;
     e->buf_range[b] = (int)j.s;
   } else {
-    TRY(gather_into(e, range_part(st), (uint32_t)b, e->s_copy));
+    TRY(gather_into(e, j.part, (uint32_t)b, e->s_copy));
     e->buf_range[b] = -1;
   }
   j.buf = b;
@@ -812,24 +798,43 @@ int process_iteration_ranges(sgw_engine *e) {
     if (st.qb > st.qa && held[s] >= 0) {
       Job j;
       j.s = s;
+      j.s_end = s + 1;
       j.action = act[s] = SGW_ACT_RESIDENT;
+      j.part = range_part(st);
       j.buf = held[s];
       j.ready = true;
       jobs.push_back(j);
     }
   }
+  long open_compact = -1;  // job that the next compacted range may join
   for (uint32_t s = 0; s < S; ++s) {
     const RangeStat &st = e->h_rstat[s];
     if (st.qb <= st.qa || held[s] >= 0) continue;
     const RangeInfo &r = e->ranges[s];
     const double E = (double)(r.e1 - r.e0), A = (double)st.act_edges;
+    uint32_t action;
+    if (E > (double)e->cap) action = SGW_ACT_SPLIT;
+    else if (E - A <= (double)st.pred * E) action = SGW_ACT_STREAM;  // extra bytes now <= predicted saving
+    else action = SGW_ACT_COMPACT;
+    act[s] = action;
+    if (action == SGW_ACT_COMPACT && open_compact >= 0) {
+      // compacted ranges whose queue segments touch share one gather and
+      // one relaxation, up to a buffer of active edges (as plain partitions)
+      Part &q = jobs[(size_t)open_compact].part;
+      if (q.from + q.size == st.qa && q.edge_count + st.act_edges <= e->cap) {
+        q.size = st.qb - q.from;
+        q.edge_count += st.act_edges;
+        jobs[(size_t)open_compact].s_end = s + 1;
+        continue;
+      }
+    }
     Job j;
     j.s = s;
-    if (E > (double)e->cap) j.action = SGW_ACT_SPLIT;
-    else if (E - A <= (double)st.pred * E) j.action = SGW_ACT_STREAM;  // extra bytes now <= predicted saving
-    else j.action = SGW_ACT_COMPACT;
-    act[s] = j.action;
+    j.s_end = s + 1;
+    j.action = action;
+    j.part = range_part(st);
     jobs.push_back(j);
+    open_compact = action == SGW_ACT_COMPACT ? (long)jobs.size() - 1 : -1;
   }
   // keep value of a buffer: predicted bytes it saves next iteration
   auto value = [&](uint32_t b) -> double {
@@ -865,7 +870,7 @@ int process_iteration_ranges(sgw_engine *e) {
       }
     }
     const RangeInfo &r = e->ranges[j.s];
-    const Part q = range_part(e->h_rstat[j.s]);
+    const Part q = j.part;
     uint32_t inner = 1;
     if (j.action == SGW_ACT_SPLIT) {
       const int b = victim(k, -1);
@@ -878,12 +883,22 @@ int process_iteration_ranges(sgw_engine *e) {
       CK(cudaStreamWaitEvent(e->s_comp, e->ev_ready[j.buf], 0));
       e->cur_streamed = (j.action == SGW_ACT_RESIDENT || j.action == SGW_ACT_STREAM) ? 1u : 0u;
       e->cur_stream_base = r.e0;
+      // a range that stays in its buffer and is predicted to be active again
+      // next iteration stops early: what further inner passes would settle
+      // is likely to be redone then, and its leftover sources cost no bytes
+      const double thr = (e->opts.sched_active_permille ? e->opts.sched_active_permille : 1u) / 1000.0;
+      const bool kept = j.action == SGW_ACT_RESIDENT || j.action == SGW_ACT_STREAM;
+      float pred = 0.0f;
+      for (uint32_t s = j.s; s < j.s_end; ++s) pred = std::max(pred, e->h_rstat[s].pred);
+      const bool cappable = kept || (e->opts.sched_flags & SGW_SCHED_CAP_COMPACT);
+      e->range_inner_cap = cappable && (double)pred >= thr ? (e->opts.sched_inner ? e->opts.sched_inner : 2u) : 0u;
       const int st = process_resident(e, q, (uint32_t)j.buf, &inner);
       e->cur_streamed = 0;
+      e->range_inner_cap = 0;
       TRY(st);
     }
     CK(cudaEventRecord(e->ev_free[j.buf], e->s_comp));
-    inner_of[j.s] = inner;
+    for (uint32_t s = j.s; s < j.s_end; ++s) inner_of[s] = inner;
     e->stats.partitions += 1;
   }
   if (e->trace_on) {
@@ -923,6 +938,9 @@ void sgw_engine_opts_default(sgw_engine_opts *o) {
   o->inner_batch = 8;
   o->tile_degree_max = 256;
   o->chunk_edges = 1024;
+  o->sched_inner = 2;
+  o->sched_active_permille = 1;
+  o->sched_flags = SGW_SCHED_CAP_COMPACT;
 }
 
 void sgw_run_params_default(sgw_run_params *p, int algo, int mode, uint32_t source) {

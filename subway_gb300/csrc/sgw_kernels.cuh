@@ -36,8 +36,6 @@ struct Ctl {
   uint32_t upd[4];           // async inner iteration k: relaxations that improved
   uint32_t wl_count[4];      // chunk-list items of inner iteration k
   uint32_t iters_run;        // inner iterations that did work
-  uint32_t dq_count[4];      // async: partition sources dirtied in inner iteration k
-  uint32_t dq_overflow[4];   //   and whether that list overflowed (then: full scan)
   uint32_t hub_active;       // single-vertex partition: the source was dirty
   uint32_t hub_value;        // single-vertex partition: its value
   uint32_t pad0;
@@ -53,8 +51,6 @@ struct Part {                // one partition of the active queue
   uint32_t edge_from;        // ptr[from]
   uint32_t first_vertex;     // queue[from]
   unsigned long long edge_count;
-  uint32_t last_vertex;      // queue[from + size - 1]
-  uint32_t pad;
 };
 
 struct WorkItem {            // a chunk of one high-degree source's edges
@@ -320,8 +316,6 @@ __global__ void k_plan(const uint32_t *ptr, const uint32_t *queue, Ctl *ctl,
       q.size = to - from;
       q.edge_from = ptr[from];
       q.first_vertex = queue[from];
-      q.last_vertex = queue[to - 1];
-      q.pad = 0;
       q.edge_count = (unsigned long long)ptr[to] - ptr[from];
       parts[p] = q;
     }
@@ -560,42 +554,16 @@ template <> struct Op<SGW_CC> {    // cc_kernel: value, atomicMin (:96-98)
   __device__ static uint32_t cand(uint32_t v, uint32_t) { return v; }
 };
 
-// Async inner iterations after the first only need the partition sources
-// that the previous iteration dirtied.  The thread whose atomicOr first sets
-// a destination's label appends it here when its id lies in the partition's
-// id range; the next iteration relaxes the listed vertices that are queued in
-// the partition (binary search in the sorted queue) instead of scanning every
-// partition source.  On overflow the next iteration scans as before.
-struct DirtyList {
-  uint32_t *out;
-  uint32_t *count;
-  uint32_t *overflow;
-  uint32_t cap;
-  uint32_t lo, hi;
-};
-
 // Relaxes one edge; returns true if the destination improved.
-template <int ALGO, bool DL = false>
+template <int ALGO>
 __device__ __forceinline__ bool relax_edge(uint32_t sval, uint32_t dst, uint32_t w,
-                                           uint32_t *value, uint8_t *nxt, const DirtyList *dl = nullptr) {
+                                           uint32_t *value, uint8_t *nxt) {
   const uint32_t c = Op<ALGO>::cand(sval, w);
   const uint32_t cur = value[dst];
   if (Op<ALGO>::kMax ? (c > cur) : (c < cur)) {
     const uint32_t old = Op<ALGO>::kMax ? atomicMax(&value[dst], c) : atomicMin(&value[dst], c);
     if (Op<ALGO>::kMax ? (c > old) : (c < old)) {
-      if (DL) {
-        // label arrays are 256-byte aligned: set the byte through its word
-        uint32_t *word = reinterpret_cast<uint32_t *>(nxt + (dst & ~3u));
-        const uint32_t sh = 8u * (dst & 3u);
-        const uint32_t prev = atomicOr(word, 1u << sh);
-        if (((prev >> sh) & 0xffu) == 0 && dst >= dl->lo && dst <= dl->hi) {
-          const uint32_t slot = atomicAdd(dl->count, 1u);
-          if (slot < dl->cap) dl->out[slot] = dst;
-          else *dl->overflow = 1u;
-        }
-      } else {
-        nxt[dst] = 1;
-      }
+      nxt[dst] = 1;
       return true;
     }
   }
@@ -648,26 +616,9 @@ struct RelaxArgs {
   uint32_t streamed;
   uint32_t stream_base;
   const uint32_t *off;
-  // async dirty lists (iteration k writes dq_out, iteration k + 1 reads it)
-  const uint32_t *dq_in;
-  uint32_t *dq_out;
-  uint32_t dq_cap;
-  uint32_t v_lo, v_hi;       // vertex ids of the partition's first and last source
 };
 
 constexpr int kRelaxThreads = 256;
-
-template <bool ASYNC>
-__device__ __forceinline__ DirtyList make_dirty_list(const RelaxArgs &a) {
-  DirtyList dl;
-  dl.out = a.dq_out;
-  dl.count = &a.ctl->dq_count[a.iter & 3u];
-  dl.overflow = &a.ctl->dq_overflow[a.iter & 3u];
-  dl.cap = a.dq_cap;
-  dl.lo = a.v_lo;
-  dl.hi = a.v_hi;
-  return dl;
-}
 
 // Tile of kRelaxThreads partition sources per CTA (grid-stride).  Each thread
 // claims one source (async: only if its label is set, clearing it), the CTA
@@ -675,63 +626,48 @@ __device__ __forceinline__ DirtyList make_dirty_list(const RelaxArgs &a) {
 // together: edge j of the tile belongs to the source found by binary search
 // in the scanned degrees.  Sources above tile_degree_max are cut into chunks
 // and appended to the chunk list instead.
+struct TileSmem {
+  uint32_t scan[kRelaxThreads + 1];
+  uint32_t boff[kRelaxThreads];
+  uint32_t val[kRelaxThreads];
+  uint32_t hub[kRelaxThreads];
+  uint32_t wsum[kRelaxThreads / 32];
+  uint32_t nhub, wbase;
+  int skip;
+};
+
 template <int ALGO, bool ASYNC, int W>
-__global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
-  __shared__ uint32_t s_scan[kRelaxThreads + 1];
-  __shared__ uint32_t s_boff[kRelaxThreads];
-  __shared__ uint32_t s_val[kRelaxThreads];
-  __shared__ uint32_t s_hub[kRelaxThreads];
-  __shared__ uint32_t s_nhub, s_wbase;
-  __shared__ int s_skip;
-  __shared__ uint32_t s_nsrc;
+__device__ __forceinline__ void relax_tile_phase(const RelaxArgs &a, TileSmem &sm) {
+  uint32_t *const s_scan = sm.scan;
+  uint32_t *const s_boff = sm.boff;
+  uint32_t *const s_val = sm.val;
+  uint32_t *const s_hub = sm.hub;
+  uint32_t &s_nhub = sm.nhub;
+  uint32_t &s_wbase = sm.wbase;
+  int &s_skip = sm.skip;
   const int tid = threadIdx.x;
   const uint32_t slot = a.iter & 3u;
-  // async iterations after the first read the previous iteration's dirty list
-  const bool listed = ASYNC && a.iter > 1 && a.dq_in != nullptr;
   if (tid == 0) {
     int skip = 0;
     if (ASYNC && a.iter > 1 && ld_acquire_u32(&a.ctl->upd[(a.iter - 1) & 3u]) == 0) skip = 1;
     s_skip = skip;
-    uint32_t nsrc = a.size;
-    if (listed) {
-      const uint32_t prev = (a.iter - 1) & 3u;
-      if (ld_acquire_u32(&a.ctl->dq_overflow[prev]) == 0)
-        nsrc = min(ld_acquire_u32(&a.ctl->dq_count[prev]), a.dq_cap);
-      else
-        nsrc = 0xffffffffu;  // overflowed: scan the partition
-    }
-    s_nsrc = nsrc;
     if (blockIdx.x == 0) {
       a.ctl->upd[(a.iter + 1) & 3u] = 0;
       a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
-      a.ctl->dq_count[(a.iter + 1) & 3u] = 0;
-      a.ctl->dq_overflow[(a.iter + 1) & 3u] = 0;
       if (!skip) atomicAdd(&a.ctl->iters_run, 1u);
     }
   }
   __syncthreads();
   if (s_skip) return;
-  const bool from_list = listed && s_nsrc != 0xffffffffu;
-  const uint32_t nsrc = from_list ? s_nsrc : a.size;
-  const DirtyList dl = make_dirty_list<ASYNC>(a);
   bool any_update = false;
-  const uint32_t ntiles = (nsrc + kRelaxThreads - 1) / kRelaxThreads;
+  const uint32_t ntiles = (a.size + kRelaxThreads - 1) / kRelaxThreads;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     if (tid == 0) s_nhub = 0;
     __syncthreads();
     const uint32_t idx = t * kRelaxThreads + tid;
-    uint32_t i = 0xffffffffu;
-    if (idx < nsrc) {
-      if (from_list) {  // a dirtied vertex: is it queued in this partition?
-        const uint32_t v = a.dq_in[idx];
-        const uint32_t pos = lower_bound_u32(a.queue + a.from, a.size, v);
-        if (pos < a.size && a.queue[a.from + pos] == v) i = a.from + pos;
-      } else {
-        i = a.from + idx;
-      }
-    }
     uint32_t d = 0, boff = 0, val = 0, u = 0;
-    if (i != 0xffffffffu) {
+    if (idx < a.size) {
+      const uint32_t i = a.from + idx;
       u = a.queue[i];
       bool act = true;
       if (ASYNC) {
@@ -789,7 +725,7 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
     {
       const int lane = tid & 31, warp = tid >> 5;
       const uint32_t incl = warp_incl_scan(d, lane);
-      __shared__ uint32_t s_wsum[kRelaxThreads / 32];
+      uint32_t *const s_wsum = sm.wsum;
       if (lane == 31) s_wsum[warp] = incl;
       __syncthreads();
       if (tid == 0) {
@@ -815,33 +751,43 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
       const uint32_t e = s_boff[k] + (j - s_scan[k]);
       uint32_t dst, w;
       load_edge<W>(a.buf, e, a.pbits, dst, w);
-      any_update |= relax_edge<ALGO, ASYNC>(s_val[k], dst, w, a.value, a.nxt, &dl);
+      any_update |= relax_edge<ALGO>(s_val[k], dst, w, a.value, a.nxt);
     }
     __syncthreads();
   }
   if (__syncthreads_or(any_update) && tid == 0) atomicAdd(&a.ctl->upd[slot], 1u);
 }
 
+template <int ALGO, bool ASYNC, int W>
+__global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
+  __shared__ TileSmem sm;
+  relax_tile_phase<ALGO, ASYNC, W>(a, sm);
+}
+
 // Chunk list of inner iteration `iter`: one warp per item.
 template <int ALGO, bool ASYNC, int W>
-__global__ void __launch_bounds__(kRelaxThreads) k_relax_chunks(RelaxArgs a) {
+__device__ __forceinline__ void relax_chunks_phase(const RelaxArgs &a) {
   const uint32_t slot = a.iter & 3u;
   if (ASYNC && a.iter > 1 && ld_acquire_u32(&a.ctl->upd[(a.iter - 1) & 3u]) == 0) return;
   const uint32_t items = min(ld_acquire_u32(&a.ctl->wl_count[slot]), a.wl_cap);
   const int lane = threadIdx.x & 31;
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  const DirtyList dl = make_dirty_list<ASYNC>(a);
   bool any_update = false;
   for (uint32_t it = gw; it < items; it += nw) {
     const WorkItem wi = a.wl[it];
     for (uint32_t j = lane; j < wi.count; j += 32) {
       uint32_t dst, w;
       load_edge<W>(a.buf, wi.boff + j, a.pbits, dst, w);
-      any_update |= relax_edge<ALGO, ASYNC>(wi.value, dst, w, a.value, a.nxt, &dl);
+      any_update |= relax_edge<ALGO>(wi.value, dst, w, a.value, a.nxt);
     }
   }
   if (__syncthreads_or(any_update) && threadIdx.x == 0) atomicAdd(&a.ctl->upd[slot], 1u);
+}
+
+template <int ALGO, bool ASYNC, int W>
+__global__ void __launch_bounds__(kRelaxThreads) k_relax_chunks(RelaxArgs a) {
+  relax_chunks_phase<ALGO, ASYNC, W>(a);
 }
 
 // Single-vertex partition (degree above the edge buffer): claim the source
@@ -1149,7 +1095,6 @@ struct RangeStat {           // one global iteration of one range
   float pred;                // predicted active edge fraction next iteration
   float feat[kMlpIn];
   uint32_t pad;
-  uint32_t last_vertex;      // queue[qb - 1]
 };
 
 // One warp per range: locate the range's queue segment, form the five
@@ -1190,7 +1135,6 @@ __global__ void k_range_stats(const RangeInfo *__restrict__ ranges, uint32_t num
     o.act_edges = act;
     o.prev_edges = act;  // becomes "previous" for the next iteration
     o.first_vertex = qb > qa ? queue[qa] : r.v0;
-    o.last_vertex = qb > qa ? queue[qb - 1] : r.v0;
     o.pred = pred;
 #pragma unroll
     for (int k = 0; k < kMlpIn; ++k) o.feat[k] = x[k];

@@ -22,6 +22,7 @@ OPT_PROFILE = 0x1
 OPT_NO_OVERLAP = 0x2
 OPT_NO_PACK = 0x4
 OPT_SCALAR_GATHER = 0x8
+SCHED_CAP_COMPACT = 0x1
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
 MODES = {"sync": SYNC, "async": ASYNC}
 
@@ -30,7 +31,8 @@ class EngineOpts(C.Structure):
     _fields_ = [("budget_bytes", C.c_uint64), ("device", C.c_int32), ("flags", C.c_uint32),
                 ("inner_batch", C.c_uint32), ("tile_degree_max", C.c_uint32),
                 ("chunk_edges", C.c_uint32), ("gather_ctas", C.c_uint32), ("num_buffers", C.c_uint32),
-                ("reserved", C.c_uint32 * 6)]
+                ("sched_inner", C.c_uint32), ("sched_active_permille", C.c_uint32),
+                ("sched_flags", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 class RunParams(C.Structure):

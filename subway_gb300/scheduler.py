@@ -84,6 +84,35 @@ def load_default(device=0):
     return N.Mlp.load(DEFAULT_MODEL, device) if DEFAULT_MODEL.exists() else None
 
 
+def mispredictions(rec: np.ndarray) -> dict:
+    """How often the predictions behind one run's decisions were wrong.
+
+    A transfer decision for range s at iteration t (stream the whole range and
+    keep it, or send only its active edges) compares the prediction p with
+    the break-even fraction 1 - A/E: streaming pays E - A extra bytes now and
+    saves the next iteration's transfer, worth y * E, where y is the range's
+    actual active edge fraction at t + 1 (0 if it is not active again).  The
+    decision was mispredicted when p and y fall on different sides of the
+    break-even point."""
+    if len(rec) == 0:
+        return {"transfer_decisions": 0, "transfer_mispredicted": 0, "prediction_mae": None}
+    nxt = {(int(r["global_iteration"]), int(r["range"])): r for r in rec}
+    dec = bad = 0
+    err = []
+    for r in rec:
+        if int(r["action"]) not in (N.ACT_STREAM, N.ACT_COMPACT):
+            continue
+        n = nxt.get((int(r["global_iteration"]) + 1, int(r["range"])))
+        y = float(n["active_edges"]) / max(1, int(n["range_edges"])) if n is not None else 0.0
+        p = float(r["predicted"])
+        even = 1.0 - float(r["active_edges"]) / max(1, int(r["range_edges"]))
+        dec += 1
+        bad += int((p >= even) != (y >= even))
+        err.append(abs(p - y))
+    return {"transfer_decisions": dec, "transfer_mispredicted": bad,
+            "prediction_mae": round(float(np.mean(err)), 4) if err else None}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=str(DEFAULT_MODEL))

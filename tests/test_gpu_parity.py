@@ -243,6 +243,20 @@ def test_transfer_forms(gpu, orc, g12w, mode, flags):
         assert np.array_equal(vals, _oracle(orc, g, algo, src)), (algo, mode)
 
 
+def test_async_inner_cap(gpu, orc, g12w):
+    """Async runs with the inner iterations of each partition visit capped
+    (the labels left over go to the next generate) give the oracle's answers."""
+    g = g12w
+    eng = gpu.Engine(g, budget_bytes=18 * g.n + 72 * 1024 + 3000 * 16)
+    src = int(g.pick_sources(1, seed=21)[0])
+    for algo in ALGS:
+        for mi in (1, 3):
+            vals, st = eng.run(algo, "async", src, max_inner=mi)
+            assert np.array_equal(vals, _oracle(orc, g, algo, src)), (algo, mi)
+            assert st["partitions"] >= st["global_iterations"] > 0
+            assert st["inner_iterations"] <= mi * st["partitions"], (algo, mi)
+
+
 def test_wide_weights_fall_back_to_full_records(gpu, orc):
     """Weights that do not fit beside the vertex id keep 8-byte records."""
     g0 = gpu.Graph.rmat(12, 8, seed=13, weighted=True)
