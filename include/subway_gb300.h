@@ -262,6 +262,8 @@ int sgw_plan_partitions(const uint32_t *ptr, uint32_t count, uint64_t cap,
 
 /* Number of CUDA devices visible (0 on a machine without a GPU). */
 int sgw_device_count(int *count);
+/* Streaming multiprocessors and global memory bytes of a device. */
+int sgw_device_info(int device, uint32_t *sm_count, uint64_t *total_bytes);
 
 /* ---- learned scheduler ------------------------------------------------------
  * No counterpart in the reference, whose only schedule is: compact every

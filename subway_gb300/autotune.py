@@ -36,19 +36,8 @@ def _time_engine(g, budget, opts, algo, mode, sources, policy, model, device, re
     return ms
 
 
-_SMS = {}
-
-
 def _sm_count(device):
-    if device not in _SMS:
-        try:
-            import subprocess
-            out = subprocess.run(["nvidia-smi", f"--id={device}", "--query-gpu=name", "--format=csv,noheader"],
-                                 capture_output=True, text=True, timeout=20).stdout
-            _SMS[device] = 152 if "GB300" in out or "B300" in out else 148
-        except Exception:  # noqa: BLE001
-            _SMS[device] = 152
-    return _SMS[device]
+    return N.device_info(device)["sm_count"]
 
 
 def tune_engine(g, budget, algo="sssp", mode="async", sources=None, policy="plain", model=None,

@@ -8,7 +8,9 @@
 //   stdout lines of subway/<app>.cu and utilities::PrintResults /
 //   SaveResults (shared/subway_utilities.cpp:4-72).
 // Extra flags: --budget BYTES (device-memory budget), --inner N (async inner
-// iterations per partition visit, 0 = until converged), --stats FILE (JSON).
+// iterations per partition visit, 0 = until converged), --stats FILE (JSON),
+// --scheduler MODEL (learned scheduling policy with this network file; the
+// answers are the same, the schedule and the bytes moved change).
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -23,7 +25,7 @@
 namespace {
 
 struct Args {
-  std::string input, output, stats;
+  std::string input, output, stats, scheduler;
   unsigned source = 0;
   int device = 0;
   unsigned long long budget = 0;
@@ -41,6 +43,7 @@ std::string help(bool can_source) {
   s += "\n    [--budget]: Device-memory budget in bytes (default: Subway's rule). E.g., --budget 1000000000";
   s += "\n    [--inner]: Async inner iterations per partition visit (default: 0 = until converged)";
   s += "\n    [--stats]: Write run statistics as JSON to this file";
+  s += "\n    [--scheduler]: Learned scheduling with this model file (e.g. subway_gb300/models/sched_mlp.bin)";
   s += "\n\n";
   return s;
 }
@@ -68,6 +71,7 @@ Args parse(int argc, char **argv, bool can_source) {
     else if (!strcmp(k, "--budget")) a.budget = strtoull(v, nullptr, 10);
     else if (!strcmp(k, "--inner")) a.inner = (unsigned)strtoul(v, nullptr, 10);
     else if (!strcmp(k, "--stats")) a.stats = v;
+    else if (!strcmp(k, "--scheduler")) a.scheduler = v;
     else {
       std::string m = std::string("\nThere was an error parsing command line argument <") + k + ">\n";
       usage_exit(can_source, m.c_str());
@@ -155,9 +159,17 @@ int main(int argc, char **argv) {
   sgw_engine_opts_default(&o);
   o.budget_bytes = a.budget;
   o.device = a.device;
+  if (!a.scheduler.empty()) o.num_buffers = 3;
   sgw_engine *e = nullptr;
   st = sgw_engine_create(g, &o, &e);
   if (st != SGW_OK) die(st, "engine");
+  sgw_mlp *model = nullptr;
+  if (!a.scheduler.empty()) {
+    st = sgw_mlp_load(a.device, a.scheduler.c_str(), &model);
+    if (st != SGW_OK) die(st, "scheduler model");
+    st = sgw_set_policy(e, SGW_POLICY_LEARNED, model);
+    if (st != SGW_OK) die(st, "scheduler policy");
+  }
   sgw_trace_enable(e, 1);
   sgw_run_params p;
   sgw_run_params_default(&p, algo, mode, a.source);
@@ -171,7 +183,16 @@ int main(int argc, char **argv) {
   st = sgw_run(e, &p, out, &s);
   if (st != SGW_OK) die(st, "run");
 
-  if (mode == SGW_ASYNC) {  // per-partition log lines (subway/sssp-async.cu:117)
+  if (mode == SGW_ASYNC && model) {  // one line per processed vertex range
+    uint64_t cnt = 0;
+    sgw_range_trace_count(e, &cnt);
+    std::vector<sgw_range_rec> tr(cnt);
+    sgw_range_trace_read(e, tr.data(), cnt, &cnt);
+    for (const auto &r : tr)
+      if (r.active_nodes)
+        printf("%u %s in Global Iteration %u, Range %u\n", r.inner_iterations,
+               r.inner_iterations > 1 ? "Inner Iterations" : "Inner Iteration", r.global_iteration, r.range);
+  } else if (mode == SGW_ASYNC) {  // per-partition log lines (subway/sssp-async.cu:117)
     uint64_t cnt = 0;
     sgw_trace_count(e, &cnt);
     std::vector<sgw_trace_rec> tr(cnt);
@@ -209,6 +230,7 @@ int main(int argc, char **argv) {
     }
   }
   sgw_engine_destroy(e);
+  if (model) sgw_mlp_destroy(model);
   sgw_graph_free(g);
   return 0;
 }

@@ -38,6 +38,7 @@ namespace {
 
 constexpr uint32_t kBInf = 4294967294u;
 constexpr int kBThreads = 256;
+constexpr uint32_t kBUnroll = 4;
 
 struct BItem {
   uint32_t u;    // source vertex
@@ -157,17 +158,29 @@ __global__ void __launch_bounds__(kBThreads) k_b_relax(const BItem *__restrict__
           }
         }
         const uint32_t cnt = min(32u, it.cnt - c);
-        for (uint32_t k = 0; k < cnt; ++k) {
-          const uint32_t dst = __shfl_sync(0xffffffffu, rd, k);
-          const uint32_t w = __shfl_sync(0xffffffffu, rw, k);
-          bool improved = false;
-          if (active) {
-            const uint32_t cand = du + (SSSP ? w : 1u);
-            uint32_t *p = &dist[(size_t)dst * L + 32 * h + lane];
-            if (cand < *p) improved = cand < atomicMin(p, cand);
+        // kBUnroll destination lines in flight per warp before the compares
+        for (uint32_t k0 = 0; k0 < cnt; k0 += kBUnroll) {
+          uint32_t dst[kBUnroll], w[kBUnroll], seen[kBUnroll];
+#pragma unroll
+          for (int q = 0; q < kBUnroll; ++q) {
+            dst[q] = __shfl_sync(0xffffffffu, rd, (k0 + q) & 31u);
+            w[q] = __shfl_sync(0xffffffffu, rw, (k0 + q) & 31u);
           }
-          const uint32_t imp = __ballot_sync(0xffffffffu, improved);
-          if (imp && lane == 0) atomicOr(&next[dst], (unsigned long long)imp << (32 * h));
+#pragma unroll
+          for (int q = 0; q < kBUnroll; ++q)
+            seen[q] = (active && k0 + q < cnt) ? dist[(size_t)dst[q] * L + 32 * h + lane] : 0u;
+#pragma unroll
+          for (int q = 0; q < kBUnroll; ++q) {
+            if (k0 + q >= cnt) break;  // uniform across the warp
+            bool improved = false;
+            if (active) {
+              const uint32_t cand = du + (SSSP ? w[q] : 1u);
+              if (cand < seen[q])
+                improved = cand < atomicMin(&dist[(size_t)dst[q] * L + 32 * h + lane], cand);
+            }
+            const uint32_t imp = __ballot_sync(0xffffffffu, improved);
+            if (imp && lane == 0) atomicOr(&next[dst[q]], (unsigned long long)imp << (32 * h));
+          }
         }
       }
     }

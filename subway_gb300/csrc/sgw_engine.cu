@@ -955,6 +955,15 @@ void sgw_run_params_default(sgw_run_params *p, int algo, int mode, uint32_t sour
   p->max_inner = 0;
 }
 
+int sgw_device_info(int device, uint32_t *sm_count, uint64_t *total_bytes) {
+  clear_error();
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device));
+  if (sm_count) *sm_count = (uint32_t)prop.multiProcessorCount;
+  if (total_bytes) *total_bytes = (uint64_t)prop.totalGlobalMem;
+  return SGW_OK;
+}
+
 int sgw_device_count(int *count) {
   if (!count) return fail(SGW_EINVAL, "null argument");
   int c = 0;

@@ -554,12 +554,13 @@ template <> struct Op<SGW_CC> {    // cc_kernel: value, atomicMin (:96-98)
   __device__ static uint32_t cand(uint32_t v, uint32_t) { return v; }
 };
 
-// Relaxes one edge; returns true if the destination improved.
+// Relaxes one edge given the destination's value as read beforehand (a
+// stale read only costs an extra atomic: values move one way); returns true
+// if the destination improved.
 template <int ALGO>
-__device__ __forceinline__ bool relax_edge(uint32_t sval, uint32_t dst, uint32_t w,
-                                           uint32_t *value, uint8_t *nxt) {
+__device__ __forceinline__ bool relax_edge_seen(uint32_t sval, uint32_t dst, uint32_t w, uint32_t cur,
+                                                uint32_t *value, uint8_t *nxt) {
   const uint32_t c = Op<ALGO>::cand(sval, w);
-  const uint32_t cur = value[dst];
   if (Op<ALGO>::kMax ? (c > cur) : (c < cur)) {
     const uint32_t old = Op<ALGO>::kMax ? atomicMax(&value[dst], c) : atomicMin(&value[dst], c);
     if (Op<ALGO>::kMax ? (c > old) : (c < old)) {
@@ -569,6 +570,18 @@ __device__ __forceinline__ bool relax_edge(uint32_t sval, uint32_t dst, uint32_t
   }
   return false;
 }
+
+template <int ALGO>
+__device__ __forceinline__ bool relax_edge(uint32_t sval, uint32_t dst, uint32_t w,
+                                           uint32_t *value, uint8_t *nxt) {
+  return relax_edge_seen<ALGO>(sval, dst, w, value[dst], value, nxt);
+}
+
+// Edges each thread keeps in flight in the expansion loops: the record and
+// destination-value loads of kRelaxUnroll edges are issued before any of
+// their compares and atomics, so a warp waits on one memory round trip per
+// kRelaxUnroll edges instead of per edge.
+constexpr int kRelaxUnroll = 4;
 
 // Whether a source with this value may push (guards u32 overflow of INF+w;
 // the reference relies on INF vertices never carrying a label).
@@ -739,19 +752,32 @@ __device__ __forceinline__ void relax_tile_phase(const RelaxArgs &a, TileSmem &s
     }
     const uint32_t total = s_scan[kRelaxThreads];
     if (tid == 0 && total) atomicAdd(&a.ctl->relaxed_edges, (unsigned long long)total);
-    for (uint32_t j = tid; j < total; j += blockDim.x) {
-      // last source k with s_scan[k] <= j (sources with d == 0 share offsets;
-      // the last one with that offset is the one that owns edge j)
-      uint32_t lo = 0, hi = kRelaxThreads;
-      while (lo < hi) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (s_scan[mid] <= j) lo = mid + 1; else hi = mid;
+    for (uint32_t j0 = tid; j0 < total; j0 += kRelaxUnroll * kRelaxThreads) {
+      uint32_t dst[kRelaxUnroll], w[kRelaxUnroll], sv[kRelaxUnroll], cur[kRelaxUnroll];
+      bool ok[kRelaxUnroll];
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q) {
+        const uint32_t j = j0 + q * kRelaxThreads;
+        ok[q] = j < total;
+        if (ok[q]) {
+          // last source k with s_scan[k] <= j (sources with d == 0 share
+          // offsets; the last one with that offset is the one that owns edge j)
+          uint32_t lo = 0, hi = kRelaxThreads;
+          while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (s_scan[mid] <= j) lo = mid + 1; else hi = mid;
+          }
+          const uint32_t k = lo - 1;
+          load_edge<W>(a.buf, s_boff[k] + (j - s_scan[k]), a.pbits, dst[q], w[q]);
+          sv[q] = s_val[k];
+        }
       }
-      const uint32_t k = lo - 1;
-      const uint32_t e = s_boff[k] + (j - s_scan[k]);
-      uint32_t dst, w;
-      load_edge<W>(a.buf, e, a.pbits, dst, w);
-      any_update |= relax_edge<ALGO>(s_val[k], dst, w, a.value, a.nxt);
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q)
+        if (ok[q]) cur[q] = a.value[dst[q]];
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q)
+        if (ok[q]) any_update |= relax_edge_seen<ALGO>(sv[q], dst[q], w[q], cur[q], a.value, a.nxt);
     }
     __syncthreads();
   }
@@ -776,10 +802,18 @@ __device__ __forceinline__ void relax_chunks_phase(const RelaxArgs &a) {
   bool any_update = false;
   for (uint32_t it = gw; it < items; it += nw) {
     const WorkItem wi = a.wl[it];
-    for (uint32_t j = lane; j < wi.count; j += 32) {
-      uint32_t dst, w;
-      load_edge<W>(a.buf, wi.boff + j, a.pbits, dst, w);
-      any_update |= relax_edge<ALGO>(wi.value, dst, w, a.value, a.nxt);
+    for (uint32_t j0 = lane; j0 < wi.count; j0 += 32 * kRelaxUnroll) {
+      uint32_t dst[kRelaxUnroll], w[kRelaxUnroll], cur[kRelaxUnroll];
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q)
+        if (j0 + 32 * q < wi.count) load_edge<W>(a.buf, wi.boff + j0 + 32 * q, a.pbits, dst[q], w[q]);
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q)
+        if (j0 + 32 * q < wi.count) cur[q] = a.value[dst[q]];
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q)
+        if (j0 + 32 * q < wi.count)
+          any_update |= relax_edge_seen<ALGO>(wi.value, dst[q], w[q], cur[q], a.value, a.nxt);
     }
   }
   if (__syncthreads_or(any_update) && threadIdx.x == 0) atomicAdd(&a.ctl->upd[slot], 1u);

@@ -90,6 +90,7 @@ _PROTOS = {
     "sgw_get_stats": (C.c_int, [_P, C.POINTER(RunStats)]),
     "sgw_plan_partitions": (C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, C.c_uint32, _u32p]),
     "sgw_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "sgw_device_info": (C.c_int, [C.c_int, _u32p, _u64p]),
     "sgw_probe_link": (C.c_int, [C.c_int, C.c_uint64, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "sgw_generate_noalloc": (C.c_int, [_P, _P, _P, C.c_uint32, C.c_int, _P, _P, _P, _u32p, _u64p]),
     "sgw_mlp_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_P)]),
@@ -158,6 +159,12 @@ def device_count() -> int:
     c = C.c_int(0)
     check(lib().sgw_device_count(C.byref(c)), "sgw_device_count")
     return c.value
+
+
+def device_info(device=0) -> dict:
+    sms, mem = C.c_uint32(0), C.c_uint64(0)
+    check(lib().sgw_device_info(device, C.byref(sms), C.byref(mem)), "sgw_device_info")
+    return {"sm_count": sms.value, "total_bytes": mem.value}
 
 
 def _ptr(a: np.ndarray) -> int:

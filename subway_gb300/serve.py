@@ -22,12 +22,14 @@ from . import native as N
 
 
 def admit(graphs, lanes, budget_bytes, device=0, chunk_edges=0):
-    """Batch objects for the graphs that fit the remaining budget, in order."""
+    """Batch objects for the graphs that fit the remaining budget, in order.
+    chunk_edges: one value for all graphs or one per graph (0 = default)."""
     left = budget_bytes
     admitted, rejected = [], []
-    for g in graphs:
+    chunks = chunk_edges if isinstance(chunk_edges, (list, tuple)) else [chunk_edges] * len(graphs)
+    for g, ch in zip(graphs, chunks):
         try:
-            b = N.Batch(g, lanes=lanes, budget_bytes=left, device=device, chunk_edges=chunk_edges)
+            b = N.Batch(g, lanes=lanes, budget_bytes=left, device=device, chunk_edges=ch)
         except N.SgwError as e:
             if e.status != -5:  # only a budget refusal means "not admitted"
                 raise
@@ -84,15 +86,25 @@ def main():
     ap.add_argument("--lanes", type=int, default=64)
     ap.add_argument("--budget", type=float, default=200e9)
     ap.add_argument("--chunk-edges", type=int, default=0)
+    ap.add_argument("--autotune", action="store_true", help="pick each graph's edges per work item by timing")
     a = ap.parse_args()
     t = time.time()
     graphs = [N.Graph.rmat(s, 16, seed=5000 + s, weighted=True, wmax=64) for s in a.scales]
     t_gen = time.time() - t
-    admitted, rejected = admit(graphs, a.lanes, int(a.budget), chunk_edges=a.chunk_edges)
+    chunks = a.chunk_edges
+    tuned = None
+    if a.autotune:
+        from .autotune import tune_batch
+        tuned = [tune_batch(g, a.algo, a.lanes) for g in graphs]
+        chunks = [best for best, _ in tuned]
+    admitted, rejected = admit(graphs, a.lanes, int(a.budget), chunk_edges=chunks)
     # warm the graphs up once
     for b in admitted:
         b.run(a.algo, np.zeros(1, np.uint32))
     res = serve(admitted, a.algo, a.queries, a.rate, lanes=a.lanes)
+    if tuned:
+        res["autotune"] = [{"scale": s, "chunk_edges": best, "trials_ms": [(c, round(ms, 2)) for c, ms in trials]}
+                           for s, (best, trials) in zip(a.scales, tuned)]
     res.update({"scales_admitted": [s for s, g in zip(a.scales, graphs) if g not in rejected],
                 "device_bytes": sum(b.device_bytes() for b in admitted), "generate_s": round(t_gen, 1)})
     print(json.dumps(res))
