@@ -67,9 +67,12 @@ def parse_args():
     ap.add_argument("--policy", default="both", choices=["plain", "learned", "both"],
                     help="both: time the plain (reference) schedule, then the learned one (headline)")
     ap.add_argument("--model", default="", help="scheduler model file; 'none' = persistence predictor")
-    ap.add_argument("--num-buffers", type=int, default=3, help="edge buffers of the learned policy")
+    ap.add_argument("--num-buffers", type=int, default=0,
+                    help="edge buffers of the learned policy (0 = sgw_sched_buffers' choice)")
     ap.add_argument("--sched-inner", type=int, default=0,
                     help="learned policy: inner-iteration cap of kept ranges predicted active (0 = library default)")
+    ap.add_argument("--sched-defer", type=int, default=0,
+                    help="learned policy: frontier per global iteration in 1/1000 of the edges (0 = whole)")
     ap.add_argument("--sched-permille", type=int, default=0,
                     help="learned policy: predicted active fraction (1/1000) that caps a kept range (0 = default)")
     return ap.parse_args()
@@ -173,7 +176,8 @@ def workload_config(a, extra=None):
          "graph": f"R-MAT(0.57,0.19,0.19,0.05) scale {a.scale}, edge factor {a.edge_factor}, "
                   "dedup, no self-loops, u32 weights in [1,64]",
          "budget_bytes": int(a.budget), "sources": a.sources, "seed": a.seed,
-         "l2": "inputs larger than L2: edges stay in host memory, vertex state ~300 MB",
+         "l2": f"inputs larger than L2: edges stay in host memory, vertex state "
+               f"~{18 * (1 << a.scale) / 1e6:.0f} MB in HBM",
          "parallelism": "replicas"}
     if extra:
         c.update(extra)
@@ -212,17 +216,18 @@ def run_ours(a, dist):
     out = np.empty(g.n, np.float32 if a.algo == "pr" else np.uint32)  # host result buffer
 
     def engine(policy):
-        nb = a.num_buffers if policy == "learned" else 0
+        nb = (a.num_buffers or N.sched_buffers(g, a.budget)) if policy == "learned" else 0
         e = N.Engine(g, budget_bytes=int(a.budget), device=dev, flags=flags, gather_ctas=a.gather_ctas,
                      tile_degree_max=a.tile_degree_max, chunk_edges=a.chunk_edges,
                      inner_batch=a.inner_batch, num_buffers=nb, sched_inner=a.sched_inner,
-                     sched_active_permille=a.sched_permille)
+                     sched_active_permille=a.sched_permille, sched_defer_permille=a.sched_defer)
         if policy == "learned":
             from subway_gb300 import scheduler
             model = None if a.model == "none" else (N.Mlp.load(a.model, dev) if a.model else
                                                      scheduler.load_default(dev))
             e.set_policy("learned", model)
             e.model_name = "persistence" if model is None else Path(a.model or scheduler.DEFAULT_MODEL).name
+        e.edge_buffers = nb or 2
         return e
 
     def measure(eng):
@@ -312,7 +317,7 @@ def run_ours(a, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": workload_config(a, {"policy": "plain" if a.policy == "plain" else "learned",
                                       "scheduler_model": getattr(eng, "model_name", None),
-                                      "edge_buffers": a.num_buffers if a.policy != "plain" else 2,
+                                      "edge_buffers": getattr(eng, "edge_buffers", 2),
                                       "transfer_record_bytes": 4 if (weighted and not a.no_pack) or not weighted else 8}),
         "plain_policy": plain_summary,
         "learned_over_plain": (None if not plain_summary else

@@ -100,6 +100,9 @@ void sgw_graph_free(sgw_graph *g);
 #define SGW_OPT_SCALAR_GATHER 0x8u
 /* sched_flags: the learned policy's inner cap also covers compacted ranges */
 #define SGW_SCHED_CAP_COMPACT 0x1u
+/* sched_flags: transfer active vertices that cannot push, as the reference's
+ * schedule does (for measuring what skipping them saves) */
+#define SGW_SCHED_KEEP_IDLE 0x2u
 
 typedef struct sgw_engine_opts {
   /* Device-memory budget in bytes for everything the engine allocates.
@@ -126,7 +129,13 @@ typedef struct sgw_engine_opts {
   uint32_t sched_inner;
   uint32_t sched_active_permille;
   uint32_t sched_flags;    /* SGW_SCHED_*                                     */
-  uint32_t reserved[3];
+  /* Learned policy: each global iteration takes the active vertices with the
+   * lowest values (highest for SSWP) up to about sched_defer_permille / 1000
+   * of the graph's edges and leaves the rest active for later iterations
+   * (0 = take the whole frontier).  Under this policy active vertices that
+   * cannot push (value INF for BFS/SSSP, 0 for SSWP) are never transferred. */
+  uint32_t sched_defer_permille;
+  uint32_t reserved[2];
 } sgw_engine_opts;
 
 void sgw_engine_opts_default(sgw_engine_opts *opts);
@@ -315,6 +324,12 @@ int sgw_mlp_load(int device, const char *path, sgw_mlp **out);
 /* Takes effect from the next run; the model's weights are copied into the
  * engine's device budget, so the model may be destroyed afterwards. */
 int sgw_set_policy(sgw_engine *e, int policy, const sgw_mlp *model);
+/* Edge buffers the learned policy should be created with for this graph and
+ * budget: 3 when a third of the edge space still holds at least 15% of the
+ * graph's edges (one range can then stay resident while two buffers keep
+ * transfers and relaxation overlapped), else 2 (larger partitions pay more
+ * than residency of a small slice). */
+int sgw_sched_buffers(const sgw_graph *g, uint64_t budget_bytes, uint32_t *num_buffers);
 
 /* Per range and global iteration of a SGW_POLICY_LEARNED run (recorded while
  * the trace is enabled): the features, the prediction and what was done. */

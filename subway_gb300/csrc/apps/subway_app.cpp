@@ -159,7 +159,7 @@ int main(int argc, char **argv) {
   sgw_engine_opts_default(&o);
   o.budget_bytes = a.budget;
   o.device = a.device;
-  if (!a.scheduler.empty()) o.num_buffers = 3;
+  if (!a.scheduler.empty() && a.budget) sgw_sched_buffers(g, a.budget, &o.num_buffers);
   sgw_engine *e = nullptr;
   st = sgw_engine_create(g, &o, &e);
   if (st != SGW_OK) die(st, "engine");

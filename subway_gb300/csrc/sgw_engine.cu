@@ -70,6 +70,7 @@ struct sgw_engine {
   uint32_t *d_buf[kMaxBuf] = {};
   double *d_pval = nullptr, *d_delta = nullptr, *d_qpush = nullptr;  // PR family
   __nv_bfloat16 *d_mlp = nullptr;          // scheduler weights (learned policy)
+  unsigned long long *d_sel_hist = nullptr; // frontier deferral histogram (learned policy)
   RangeInfo *d_ranges = nullptr;           // static vertex ranges of this family
   RangeStat *d_rstat = nullptr;            // per-range statistics, one iteration
   int fam = 0;
@@ -185,7 +186,7 @@ int read_ctl(sgw_engine *e) {
 enum Family { FAM_INT = 0, FAM_PR = 1 };
 
 struct Layout {
-  size_t off, tflag, tagg, tincl, ctl, mlp;           // common
+  size_t off, tflag, tagg, tincl, ctl, mlp, sel;      // common
   size_t value, l1, l2, queue, ptr, delta, qpush;     // family
   size_t parts, ranges, rstat, wl, buf[kMaxBuf], total;
   uint64_t cap;
@@ -203,6 +204,7 @@ Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
   L.tincl = take(8ull * num_tiles);
   L.ctl = take(sizeof(Ctl));
   L.mlp = take(sizeof(__nv_bfloat16) * kMlpParams);
+  L.sel = take(sizeof(unsigned long long) * kSelBins);
   if (fam == FAM_INT) {
     L.value = take(4ull * n);
     L.l1 = take(n);
@@ -274,6 +276,7 @@ int carve(sgw_engine *e, int fam, uint64_t cap) {
   e->d_ranges = (RangeInfo *)(b + L.ranges);
   e->d_rstat = (RangeStat *)(b + L.rstat);
   e->d_mlp = (__nv_bfloat16 *)(b + L.mlp);
+  e->d_sel_hist = (unsigned long long *)(b + L.sel);
   e->d_wl = (WorkItem *)(b + L.wl);
   for (int i = 0; i < kMaxBuf; ++i) e->d_buf[i] = (uint32_t *)(b + L.buf[i]);
   e->cap = L.cap;
@@ -319,6 +322,31 @@ uint32_t grid_for(const sgw_engine *e, uint64_t items, uint32_t per_cta) {
   return (uint32_t)std::max<uint64_t>(1, std::min(g, mx));
 }
 
+// Frontier deferral: value range, degree histogram and the selected bin of
+// the pushable active vertices, all on the device (the generate reads the
+// result from the control block).
+int launch_select(sgw_engine *e) {
+  const int algo = e->params.algo;
+  size_t slot = 0;
+  TRY(prof_begin(e, K_GENERATE, e->s_comp, &slot));
+  CK(cudaMemsetAsync(&e->d_ctl->sel_lo, 0xff, sizeof(uint32_t), e->s_comp));
+  CK(cudaMemsetAsync(&e->d_ctl->sel_hi, 0, sizeof(uint32_t), e->s_comp));
+  CK(cudaMemsetAsync(e->d_sel_hist, 0, sizeof(unsigned long long) * kSelBins, e->s_comp));
+  const uint32_t grid = grid_for(e, (e->n + 15) / 16, 256);
+  k_select_range<<<grid, 256, 0, e->s_comp>>>(e->n, algo, e->d_l1, e->d_l2, e->d_off, e->d_value, e->d_ctl);
+  CK(cudaGetLastError());
+  k_select_hist<<<grid, 256, 0, e->s_comp>>>(e->n, algo, e->d_l1, e->d_l2, e->d_off, e->d_value, e->d_ctl,
+                                             e->d_sel_hist);
+  CK(cudaGetLastError());
+  const unsigned long long target =
+      (unsigned long long)((double)e->m * (double)e->opts.sched_defer_permille / 1000.0);
+  k_select_pick<<<1, kSelBins / 4, 0, e->s_comp>>>(algo, e->d_sel_hist, target, e->d_ctl);
+  CK(cudaGetLastError());
+  TRY(prof_end(e, e->s_comp, slot));
+  e->stats.launches += 3;
+  return SGW_OK;
+}
+
 int launch_generate(sgw_engine *e, int consume) {
   GenArgs a;
   a.n = e->n;
@@ -341,6 +369,17 @@ int launch_generate(sgw_engine *e, int consume) {
   a.qpush = e->d_qpush;
   a.acc = (double)e->params.pr_acc;
   a.damping = (double)e->params.pr_damping;
+  if (e->policy == SGW_POLICY_LEARNED && e->fam == FAM_INT) {
+    // learned policy: never queue vertices that cannot push, and with a
+    // deferral target take the frontier lowest values first (highest: SSWP)
+    a.sel_mode = (e->opts.sched_flags & SGW_SCHED_KEEP_IDLE) ? 0 : 1;
+    a.algo = e->params.algo;
+    a.value = e->d_value;
+    if (e->opts.sched_defer_permille) {
+      a.sel_mode |= 2;
+      TRY(launch_select(e));
+    }
+  }
   CK(cudaMemsetAsync(&e->d_ctl->num_seen, 0, sizeof(uint32_t), e->s_comp));
   size_t slot = 0;
   TRY(prof_begin(e, K_GENERATE, e->s_comp, &slot));
@@ -806,17 +845,38 @@ int process_iteration_ranges(sgw_engine *e) {
       jobs.push_back(j);
     }
   }
-  long open_compact = -1;  // job that the next compacted range may join
+  // Streaming a whole range pays E - A extra bytes now and saves the next
+  // iteration's transfer (predicted p * E) only if the range then is still
+  // in a buffer.  Two buffers keep the transfer/relax pipeline going, so at
+  // most num_buffers - 2 ranges can stay: stream the ranges with the largest
+  // predicted net saving, up to that many; send the others compacted.
+  std::vector<std::pair<double, uint32_t>> stream_cand;
   for (uint32_t s = 0; s < S; ++s) {
     const RangeStat &st = e->h_rstat[s];
     if (st.qb <= st.qa || held[s] >= 0) continue;
     const RangeInfo &r = e->ranges[s];
     const double E = (double)(r.e1 - r.e0), A = (double)st.act_edges;
-    uint32_t action;
-    if (E > (double)e->cap) action = SGW_ACT_SPLIT;
-    else if (E - A <= (double)st.pred * E) action = SGW_ACT_STREAM;  // extra bytes now <= predicted saving
-    else action = SGW_ACT_COMPACT;
-    act[s] = action;
+    if (E > (double)e->cap) act[s] = SGW_ACT_SPLIT;
+    else if (E - A <= (double)st.pred * E) {
+      act[s] = SGW_ACT_STREAM;
+      stream_cand.push_back({(double)st.pred * E - (E - A), s});
+    } else {
+      act[s] = SGW_ACT_COMPACT;
+    }
+  }
+  const size_t keep_slots = e->nbuf > 2 ? e->nbuf - 2 : 0;
+  if (stream_cand.size() > keep_slots) {
+    std::sort(stream_cand.begin(), stream_cand.end(),
+              [](const std::pair<double, uint32_t> &x, const std::pair<double, uint32_t> &y) {
+                return x.first > y.first || (x.first == y.first && x.second < y.second);
+              });
+    for (size_t k = keep_slots; k < stream_cand.size(); ++k) act[stream_cand[k].second] = SGW_ACT_COMPACT;
+  }
+  long open_compact = -1;  // job that the next compacted range may join
+  for (uint32_t s = 0; s < S; ++s) {
+    const RangeStat &st = e->h_rstat[s];
+    if (st.qb <= st.qa || held[s] >= 0) continue;
+    const uint32_t action = act[s];
     if (action == SGW_ACT_COMPACT && open_compact >= 0) {
       // compacted ranges whose queue segments touch share one gather and
       // one relaxation, up to a buffer of active edges (as plain partitions)
@@ -1256,6 +1316,17 @@ int sgw_process_partition(sgw_engine *e, uint32_t i, uint32_t *inner_iterations)
   if (i == 0) e->gitr += 1;
   trace_partition(e, i, iters);
   if (inner_iterations) *inner_iterations = iters;
+  return SGW_OK;
+}
+
+int sgw_sched_buffers(const sgw_graph *g, uint64_t budget_bytes, uint32_t *num_buffers) {
+  clear_error();
+  if (!g || !num_buffers) return fail(SGW_EINVAL, "null argument");
+  uint32_t bits = 0;
+  const double rec = g->weighted && !pack_bits(g, &bits) ? 8.0 : 4.0;
+  const double space = (double)budget_bytes - 18.0 * (double)g->n;  // integer vertex state
+  const double third = space > 0 ? space / 3.0 / rec : 0.0;
+  *num_buffers = (g->m > 0 && third >= 0.15 * (double)g->m) ? 3u : 2u;
   return SGW_OK;
 }
 

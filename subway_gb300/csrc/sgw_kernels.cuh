@@ -38,6 +38,8 @@ struct Ctl {
   uint32_t iters_run;        // inner iterations that did work
   uint32_t hub_active;       // single-vertex partition: the source was dirty
   uint32_t hub_value;        // single-vertex partition: its value
+  uint32_t sel_lo, sel_hi;   // deferral: value range of the pushable active vertices
+  uint32_t sel_bin;          //   and the last value bin selected this iteration
   uint32_t pad0;
   unsigned long long reached_edges;
   unsigned long long relaxed_edges;
@@ -169,7 +171,36 @@ struct GenArgs {
   double *qpush;             // per queued vertex: damping * delta / outdeg
   double acc;
   double damping;
+  // Value-aware selection (integer algorithms, learned policy), bit flags:
+  // 1: active vertices that cannot push (BFS/SSSP value INF, SSWP value 0)
+  //    are dropped like degree-0 ones, since relaxing them changes nothing;
+  // 2: active vertices whose value lies beyond the bin chosen by
+  //    k_select_pick are deferred (labels kept, not queued).
+  int sel_mode = 0;
+  int algo = 0;
+  const uint32_t *value = nullptr;
 };
+
+// Whether a vertex with this value produces candidates when relaxed.
+__device__ __forceinline__ bool pushable(int algo, uint32_t v) {
+  if (algo == SGW_BFS || algo == SGW_SSSP) return v != kInf;
+  if (algo == SGW_SSWP) return v != 0;
+  return true;
+}
+
+// Deferral bins: kSelBins equal slices of [lo, hi]; min-algorithms take the
+// lowest values first, SSWP (max) the highest.  Values outside [lo, hi] (set
+// after the histogram was taken) count as selected when they are better.
+constexpr uint32_t kSelBins = 1024;
+__device__ __forceinline__ uint32_t sel_bin_of(uint32_t v, uint32_t lo, uint32_t hi) {
+  return (uint32_t)(((unsigned long long)(v - lo) * kSelBins) / ((unsigned long long)(hi - lo) + 1ull));
+}
+__device__ __forceinline__ bool selected(int algo, uint32_t v, uint32_t lo, uint32_t hi, uint32_t bin) {
+  if (v < lo) return algo != SGW_SSWP;
+  if (v > hi) return algo == SGW_SSWP;
+  const uint32_t b = sel_bin_of(v, lo, hi);
+  return algo == SGW_SSWP ? b >= bin : b <= bin;
+}
 
 // One CTA per 4096-vertex tile.  Each warp owns 512 consecutive vertices,
 // 32 per round: a lane reads label1|label2 of its vertex, the warp ballots the
@@ -201,10 +232,16 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
   uint32_t keepmask[kGenRounds];
   double push[PR ? kGenRounds : 1];
   uint32_t wcount = 0, wedges = 0, seen = 0;
+  uint32_t sel_lo = 0, sel_hi = 0, sel_bin = 0;
+  if (!PR && (a.sel_mode & 2)) {
+    sel_lo = a.ctl->sel_lo;
+    sel_hi = a.ctl->sel_hi;
+    sel_bin = a.ctl->sel_bin;
+  }
 #pragma unroll
   for (int r = 0; r < kGenRounds; ++r) {
     const uint32_t v = wbase + r * 32 + lane;
-    bool act = false;
+    bool act = false, defer = false;
     uint32_t d = 0;
     if (PR) {
       push[PR ? r : 0] = 0.0;
@@ -222,11 +259,18 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
       act = (a.l1[v] | a.l2[v]) != 0;
       if (act) {
         d = __ldg(&a.off[v + 1]) - __ldg(&a.off[v]);
-        if (a.consume || d == 0) { a.l1[v] = 0; a.l2[v] = 0; }
+        bool drop = d == 0;
+        if (a.sel_mode && !drop) {
+          const uint32_t val = a.value[v];
+          if (!pushable(a.algo, val)) drop = (a.sel_mode & 1) != 0;
+          else if ((a.sel_mode & 2) && !selected(a.algo, val, sel_lo, sel_hi, sel_bin)) defer = true;
+        }
+        if (!defer && (a.consume || drop)) { a.l1[v] = 0; a.l2[v] = 0; }
+        if (drop) d = 0;
       }
     }
     seen += __popc(__ballot_sync(0xffffffffu, act));
-    const bool keep = act && d > 0;
+    const bool keep = act && d > 0 && !defer;
     keepmask[r] = __ballot_sync(0xffffffffu, keep);
     deg[r] = keep ? d : 0;
     wcount += __popc(keepmask[r]);
@@ -278,6 +322,124 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
       a.ctl->tile_done = 0;
     }
   }
+}
+
+// ---- frontier deferral (learned policy) --------------------------------------
+// Before a generate, three small passes pick how much of the frontier to take:
+// the value range of the pushable active vertices, a histogram of their
+// out-degrees over kSelBins value bins, and the bin at which the cumulative
+// degree reaches the target (lowest values first; highest for SSWP).  The
+// generate then queues only the selected vertices; the rest keep their labels
+// for a later iteration.  Relaxing far vertices first wastes their edges'
+// transfer when they improve again later; this is the delta-stepping idea
+// applied to out-of-memory partitions.
+// Visits the pushable active vertices of degree > 0: each thread reads the
+// two label arrays 16 bytes at a time (label arrays are 256-byte aligned),
+// so a pass over n vertices keeps enough loads in flight to run at memory
+// speed; only active vertices read their pointers and value.
+template <class F>
+__device__ __forceinline__ void for_sel_candidates(uint32_t n, int algo, const uint8_t *l1, const uint8_t *l2,
+                                                   const uint32_t *off, const uint32_t *value, F f) {
+  const uint32_t nvec = n / 16u;
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  auto visit = [&](uint32_t v) {
+    const uint32_t deg = __ldg(&off[v + 1]) - __ldg(&off[v]);
+    if (deg == 0) return;
+    const uint32_t val = value[v];
+    if (pushable(algo, val)) f(val, deg);
+  };
+  for (uint32_t i = tid; i < nvec; i += nth) {
+    const uint4 a = reinterpret_cast<const uint4 *>(l1)[i];
+    const uint4 b = reinterpret_cast<const uint4 *>(l2)[i];
+    const uint32_t w[4] = {a.x | b.x, a.y | b.y, a.z | b.z, a.w | b.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (w[q] == 0) continue;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if ((w[q] >> (8 * k)) & 0xffu) visit(16u * i + 4u * q + k);
+    }
+  }
+  for (uint32_t v = 16u * nvec + tid; v < n; v += nth)
+    if ((l1[v] | l2[v]) != 0) visit(v);
+}
+
+__global__ void __launch_bounds__(256) k_select_range(uint32_t n, int algo, const uint8_t *l1, const uint8_t *l2,
+                                                      const uint32_t *off, const uint32_t *value, Ctl *ctl) {
+  uint32_t lo = 0xffffffffu, hi = 0u;
+  for_sel_candidates(n, algo, l1, l2, off, value, [&](uint32_t val, uint32_t) {
+    lo = min(lo, val);
+    hi = max(hi, val);
+  });
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if ((threadIdx.x & 31) == 0 && lo <= hi) {
+    atomicMin(&ctl->sel_lo, lo);
+    atomicMax(&ctl->sel_hi, hi);
+  }
+}
+
+// Per-CTA bins in shared memory (per-CTA sums stay below m < 2^32), added
+// into 64-bit global bins at the end.
+__global__ void __launch_bounds__(256) k_select_hist(uint32_t n, int algo, const uint8_t *l1, const uint8_t *l2,
+                                                     const uint32_t *off, const uint32_t *value, const Ctl *ctl,
+                                                     unsigned long long *hist) {
+  __shared__ uint32_t s_hist[kSelBins];
+  for (uint32_t i = threadIdx.x; i < kSelBins; i += blockDim.x) s_hist[i] = 0u;
+  __syncthreads();
+  const uint32_t lo = ctl->sel_lo, hi = ctl->sel_hi;
+  if (lo <= hi)
+    for_sel_candidates(n, algo, l1, l2, off, value,
+                       [&](uint32_t val, uint32_t deg) { atomicAdd(&s_hist[sel_bin_of(val, lo, hi)], deg); });
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < kSelBins; i += blockDim.x)
+    if (s_hist[i]) atomicAdd(&hist[i], (unsigned long long)s_hist[i]);
+}
+
+// One CTA of kSelBins / 4 threads: cumulative degree over the bins in
+// selection order; sel_bin = first bin at which it reaches `target`.
+__global__ void __launch_bounds__(kSelBins / 4) k_select_pick(int algo, const unsigned long long *hist,
+                                                              unsigned long long target, Ctl *ctl) {
+  __shared__ unsigned long long s_part[kSelBins / 4 / 32];
+  __shared__ uint32_t s_k;  // first position (selection order) reaching the target
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool rev = algo == SGW_SSWP;
+  if (tid == 0) s_k = kSelBins - 1u;  // target never reached: take everything
+  // thread t owns 4 consecutive bins in selection order
+  unsigned long long h[4], mine = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const uint32_t k = 4u * tid + q;
+    h[q] = hist[rev ? kSelBins - 1u - k : k];
+    mine += h[q];
+  }
+  unsigned long long incl = mine;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_part[warp] = incl;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long acc = 0;
+    for (int w = 0; w < (int)(kSelBins / 4 / 32); ++w) {
+      const unsigned long long x = s_part[w];
+      s_part[w] = acc;
+      acc += x;
+    }
+  }
+  __syncthreads();
+  unsigned long long run = s_part[warp] + incl - mine;
+  uint32_t first = 0xffffffffu;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    run += h[q];
+    if (first == 0xffffffffu && h[q] && run >= target) first = 4u * tid + q;
+  }
+  if (first != 0xffffffffu) atomicMin(&s_k, first);
+  __syncthreads();
+  if (tid == 0) ctl->sel_bin = rev ? kSelBins - 1u - s_k : s_k;
 }
 
 // ---- partition planner ------------------------------------------------------

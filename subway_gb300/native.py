@@ -23,6 +23,7 @@ OPT_NO_OVERLAP = 0x2
 OPT_NO_PACK = 0x4
 OPT_SCALAR_GATHER = 0x8
 SCHED_CAP_COMPACT = 0x1
+SCHED_KEEP_IDLE = 0x2
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
 MODES = {"sync": SYNC, "async": ASYNC}
 
@@ -32,7 +33,8 @@ class EngineOpts(C.Structure):
                 ("inner_batch", C.c_uint32), ("tile_degree_max", C.c_uint32),
                 ("chunk_edges", C.c_uint32), ("gather_ctas", C.c_uint32), ("num_buffers", C.c_uint32),
                 ("sched_inner", C.c_uint32), ("sched_active_permille", C.c_uint32),
-                ("sched_flags", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("sched_flags", C.c_uint32), ("sched_defer_permille", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 class RunParams(C.Structure):
@@ -103,6 +105,7 @@ _PROTOS = {
     "sgw_mlp_save": (C.c_int, [_P, C.c_char_p]),
     "sgw_mlp_load": (C.c_int, [C.c_int, C.c_char_p, C.POINTER(_P)]),
     "sgw_set_policy": (C.c_int, [_P, C.c_int, _P]),
+    "sgw_sched_buffers": (C.c_int, [_P, C.c_uint64, _u32p]),
     "sgw_batch_create": (C.c_int, [_P, C.POINTER(EngineOpts), C.c_uint32, C.POINTER(_P)]),
     "sgw_batch_destroy": (C.c_int, [_P]),
     "sgw_batch_device_bytes": (C.c_int, [_P, _u64p]),
@@ -165,6 +168,13 @@ def device_info(device=0) -> dict:
     sms, mem = C.c_uint32(0), C.c_uint64(0)
     check(lib().sgw_device_info(device, C.byref(sms), C.byref(mem)), "sgw_device_info")
     return {"sm_count": sms.value, "total_bytes": mem.value}
+
+
+def sched_buffers(graph, budget_bytes) -> int:
+    """Edge buffers for a learned-policy engine on this graph and budget."""
+    nb = C.c_uint32(0)
+    check(lib().sgw_sched_buffers(graph.h, int(budget_bytes), C.byref(nb)), "sgw_sched_buffers")
+    return nb.value
 
 
 def _ptr(a: np.ndarray) -> int:

@@ -73,13 +73,15 @@ def _oracle(orc, g, algo, src):
 
 
 @pytest.mark.parametrize("model_kind", ["persistence", "random"])
-@pytest.mark.parametrize("num_buffers", [2, 3])
-def test_learned_policy_bit_exact(gpu, orc, model_kind, num_buffers):
+@pytest.mark.parametrize("num_buffers,defer", [(2, 0), (3, 0), (3, 30), (4, 200)])
+def test_learned_policy_bit_exact(gpu, orc, model_kind, num_buffers, defer):
+    """Any network, buffer count and frontier deferral target: the answers
+    are the oracle's."""
     g = gpu.Graph.rmat(12, 16, seed=31, weighted=True)
     model = gpu.Mlp.create(0, seed=9) if model_kind == "random" else None
     for edges_budget in (400, 6000, 60000):
         eng = gpu.Engine(g, budget_bytes=18 * g.n + 96 * 1024 + edges_budget * 4 * num_buffers,
-                         num_buffers=num_buffers)
+                         num_buffers=num_buffers, sched_defer_permille=defer)
         eng.set_policy("learned", model)
         src = int(g.pick_sources(1, seed=edges_budget)[0])
         for algo in ("bfs", "sssp", "sswp", "cc"):
@@ -106,7 +108,7 @@ def test_learned_policy_uses_residency(gpu):
     g = gpu.Graph.rmat(14, 16, seed=33, weighted=True)
     budget = 18 * g.n + 96 * 1024 + int(0.4 * g.m) * 4 * 2
     plain = gpu.Engine(g, budget_bytes=budget)
-    learned = gpu.Engine(g, budget_bytes=budget, sched_active_permille=2000)
+    learned = gpu.Engine(g, budget_bytes=budget, sched_active_permille=2000, num_buffers=3)
     learned.set_policy("learned")
     learned.trace_enable(True)
     src = int(g.pick_sources(1, seed=1)[0])
@@ -116,7 +118,7 @@ def test_learned_policy_uses_residency(gpu):
     rec = learned.range_trace()
     assert (rec["action"] == gpu.ACT_RESIDENT).any()
     assert s2["h2d_bytes"] <= s1["h2d_bytes"]
-    capped = gpu.Engine(g, budget_bytes=budget, sched_active_permille=1, sched_inner=1)
+    capped = gpu.Engine(g, budget_bytes=budget, sched_active_permille=1, sched_inner=1, num_buffers=3)
     capped.set_policy("learned")
     capped.trace_enable(True)
     v3, s3 = capped.run("sssp", "async", src)
