@@ -131,9 +131,11 @@ typedef struct sgw_engine_opts {
   uint32_t sched_flags;    /* SGW_SCHED_*                                     */
   /* Learned policy: each global iteration takes the active vertices with the
    * lowest values (highest for SSWP) up to about sched_defer_permille / 1000
-   * of the graph's edges and leaves the rest active for later iterations
-   * (0 = take the whole frontier).  Under this policy active vertices that
-   * cannot push (value INF for BFS/SSSP, 0 for SSWP) are never transferred. */
+   * of the graph's edges and leaves the rest active for later iterations.
+   * 0 = automatic: 250 when the graph's edge records exceed four times the
+   * edge-buffer space, else the whole frontier; above 1000 = always the
+   * whole frontier.  Under this policy active vertices that cannot push
+   * (value INF for BFS/SSSP, 0 for SSWP) are never transferred. */
   uint32_t sched_defer_permille;
   uint32_t reserved[2];
 } sgw_engine_opts;

@@ -322,6 +322,18 @@ uint32_t grid_for(const sgw_engine *e, uint64_t items, uint32_t per_cta) {
   return (uint32_t)std::max<uint64_t>(1, std::min(g, mx));
 }
 
+// Deferral target in 1/1000 of the edges (0 = whole frontier).  Automatic:
+// defer when the edges are far larger than what the buffers hold, where each
+// avoided re-transfer is worth more than the selection passes cost.
+uint32_t defer_permille(const sgw_engine *e) {
+  const uint32_t o = e->opts.sched_defer_permille;
+  if (o > 1000) return 0;
+  if (o) return o;
+  const double edges = (double)e->m * 4.0 * e->W;
+  const double space = (double)e->nbuf * (double)e->cap * 4.0 * e->W;
+  return edges > 4.0 * space ? 250u : 0u;
+}
+
 // Frontier deferral: value range, degree histogram and the selected bin of
 // the pushable active vertices, all on the device (the generate reads the
 // result from the control block).
@@ -338,8 +350,7 @@ int launch_select(sgw_engine *e) {
   k_select_hist<<<grid, 256, 0, e->s_comp>>>(e->n, algo, e->d_l1, e->d_l2, e->d_off, e->d_value, e->d_ctl,
                                              e->d_sel_hist);
   CK(cudaGetLastError());
-  const unsigned long long target =
-      (unsigned long long)((double)e->m * (double)e->opts.sched_defer_permille / 1000.0);
+  const unsigned long long target = (unsigned long long)((double)e->m * (double)defer_permille(e) / 1000.0);
   k_select_pick<<<1, kSelBins / 4, 0, e->s_comp>>>(algo, e->d_sel_hist, target, e->d_ctl);
   CK(cudaGetLastError());
   TRY(prof_end(e, e->s_comp, slot));
@@ -375,7 +386,7 @@ int launch_generate(sgw_engine *e, int consume) {
     a.sel_mode = (e->opts.sched_flags & SGW_SCHED_KEEP_IDLE) ? 0 : 1;
     a.algo = e->params.algo;
     a.value = e->d_value;
-    if (e->opts.sched_defer_permille) {
+    if (defer_permille(e)) {
       a.sel_mode |= 2;
       TRY(launch_select(e));
     }

@@ -6,12 +6,18 @@
 //                into the active queue (replaces prePrefix, thrust::reduce,
 //                two thrust::exclusive_scan, makeQueue, makeActiveNodesPointer)
 //   k_plan       greedy partition boundaries on the device (Partitioner)
-//   k_gather     active-edge gather from mapped pinned host CSR into an HBM
-//                edge buffer (replaces the host std::thread copy dynamic<E>)
+//   k_gather_v   active-edge gather from the engine's mapped pinned transfer
+//                copy of the edges into an HBM edge buffer, 16-byte reads
+//                (replaces the host std::thread copy dynamic<E>); k_gather
+//                is the one-record-per-thread form
 //   k_relax_tile CTA-cooperative expansion of a tile of frontier sources
 //                staged in shared memory (bfs/sssp/sswp/cc kernels, sync and
 //                async forms)
 //   k_relax_chunks warp-per-chunk expansion of high-degree sources
+// Learned policy only (no reference counterpart):
+//   k_select_*   value range, degree histogram and cut of the frontier when
+//                far vertices are deferred
+//   k_range_stats per-range features and the scheduler network's forward pass
 #pragma once
 
 #include <cuda_runtime.h>
