@@ -98,6 +98,9 @@ void sgw_graph_free(sgw_graph *g);
 #define SGW_OPT_NO_PACK    0x4u
 /* Gather host records one per thread instead of as aligned 16-byte words. */
 #define SGW_OPT_SCALAR_GATHER 0x8u
+/* Expand frontier edges in CTA tiles of 256 sources (k_relax_tile) instead
+ * of warp tiles of 32 (k_relax_warp). */
+#define SGW_OPT_CTA_TILES 0x10u
 /* sched_flags: the learned policy's inner cap also covers compacted ranges */
 #define SGW_SCHED_CAP_COMPACT 0x1u
 /* sched_flags: transfer active vertices that cannot push, as the reference's

@@ -520,7 +520,8 @@ int launch_relax_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, u
   a.stream_base = e->cur_stream_base;
   a.off = e->d_off;
   const uint32_t g1 = grid_for(e, q.size, kRelaxThreads);
-  k_relax_tile<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
+  if (e->opts.flags & SGW_OPT_CTA_TILES) k_relax_tile<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
+  else k_relax_warp<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
   CK(cudaGetLastError());
   k_relax_chunks<ALGO, ASYNC, W><<<e->num_sms * 4, kRelaxThreads, 0, e->s_comp>>>(a);
   CK(cudaGetLastError());

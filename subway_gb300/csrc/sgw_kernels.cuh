@@ -958,6 +958,138 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
   relax_tile_phase<ALGO, ASYNC, W>(a, sm);
 }
 
+// Warp-tile form of k_relax_tile: each warp takes 32 partition sources at a
+// time and expands their edges on its own (warp scan of the degrees, owner
+// found by binary search in the warp's slice of shared memory), so warps
+// never wait on each other inside the loop; the CTA meets once at the end to
+// publish its counters.  Sources above tile_degree_max go to the chunk list
+// as in the CTA form.
+constexpr int kWarpsPerCta = kRelaxThreads / 32;
+template <int ALGO, bool ASYNC, int W>
+__global__ void __launch_bounds__(kRelaxThreads, 5) k_relax_warp(RelaxArgs a) {
+  __shared__ uint32_t s_excl[kWarpsPerCta][33];
+  __shared__ uint32_t s_boff[kWarpsPerCta][32];
+  __shared__ uint32_t s_val[kWarpsPerCta][32];
+  __shared__ int s_skip;
+  __shared__ unsigned long long s_edges, s_srcs;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const uint32_t slot = a.iter & 3u;
+  if (tid == 0) {
+    int skip = 0;
+    if (ASYNC && a.iter > 1 && ld_acquire_u32(&a.ctl->upd[(a.iter - 1) & 3u]) == 0) skip = 1;
+    s_skip = skip;
+    s_edges = 0;
+    s_srcs = 0;
+    if (blockIdx.x == 0) {
+      a.ctl->upd[(a.iter + 1) & 3u] = 0;
+      a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
+      if (!skip) atomicAdd(&a.ctl->iters_run, 1u);
+    }
+  }
+  __syncthreads();
+  if (s_skip) return;
+  uint32_t *const excl_s = s_excl[wid];
+  uint32_t *const boff_s = s_boff[wid];
+  uint32_t *const val_s = s_val[wid];
+  bool any_update = false;
+  unsigned long long my_edges = 0, my_srcs = 0;
+  const uint32_t ntiles = (a.size + 31u) / 32u;
+  const uint32_t gw = blockIdx.x * kWarpsPerCta + wid, nw = gridDim.x * kWarpsPerCta;
+  for (uint32_t t = gw; t < ntiles; t += nw) {
+    const uint32_t idx = t * 32u + lane;
+    uint32_t d = 0, boff = 0, val = 0;
+    if (idx < a.size) {
+      const uint32_t i = a.from + idx;
+      const uint32_t u = a.queue[i];
+      bool act = true;
+      if (ASYNC) {
+        act = a.cur[u] != 0;
+        if (act) a.cur[u] = 0;
+      }
+      if (act) {
+        val = a.value[u];
+        if (can_push<ALGO>(val)) {
+          const uint32_t p0 = a.ptr[i];
+          d = a.ptr[i + 1] - p0;
+          boff = a.streamed ? a.off[u] - a.stream_base : p0 - a.edge_from;
+        }
+      }
+    }
+    my_srcs += __popc(__ballot_sync(0xffffffffu, d > 0));
+    // high-degree sources: the warp writes their chunk items together
+    unsigned hubs = __ballot_sync(0xffffffffu, d > a.tile_degree_max);
+    while (hubs) {
+      const int h = __ffs(hubs) - 1;
+      hubs &= hubs - 1;
+      const uint32_t hd = __shfl_sync(0xffffffffu, d, h);
+      const uint32_t hb = __shfl_sync(0xffffffffu, boff, h);
+      const uint32_t hv = __shfl_sync(0xffffffffu, val, h);
+      const uint32_t nch = (hd + a.chunk_edges - 1) / a.chunk_edges;
+      uint32_t wb = 0;
+      if (lane == 0) wb = atomicAdd(&a.ctl->wl_count[slot], nch);
+      wb = __shfl_sync(0xffffffffu, wb, 0);
+      for (uint32_t c = lane; c < nch; c += 32) {
+        if (wb + c < a.wl_cap) {
+          WorkItem it;
+          it.boff = hb + c * a.chunk_edges;
+          it.count = min(a.chunk_edges, hd - c * a.chunk_edges);
+          it.value = hv;
+          it.vertex = 0;
+          a.wl[wb + c] = it;
+        } else {
+          atomicExch(&a.ctl->error, 3u);
+        }
+      }
+      my_edges += hd;
+    }
+    if (d > a.tile_degree_max) d = 0;
+    const uint32_t incl = warp_incl_scan(d, lane);
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    excl_s[lane] = incl - d;
+    boff_s[lane] = boff;
+    val_s[lane] = val;
+    __syncwarp();
+    my_edges += total;
+    for (uint32_t j0 = lane; j0 < total; j0 += 32u * kRelaxUnroll) {
+      uint32_t dst[kRelaxUnroll], w[kRelaxUnroll], sv[kRelaxUnroll], cur[kRelaxUnroll];
+      bool ok[kRelaxUnroll];
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q) {
+        const uint32_t j = j0 + 32u * q;
+        ok[q] = j < total;
+        if (ok[q]) {
+          // last lane k with excl[k] <= j (lanes with d == 0 share offsets;
+          // the last one with that offset owns edge j)
+          uint32_t lo = 0, hi = 32;
+          while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (excl_s[mid] <= j) lo = mid + 1; else hi = mid;
+          }
+          const uint32_t k = lo - 1;
+          load_edge<W>(a.buf, boff_s[k] + (j - excl_s[k]), a.pbits, dst[q], w[q]);
+          sv[q] = val_s[k];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q)
+        if (ok[q]) cur[q] = a.value[dst[q]];
+#pragma unroll
+      for (int q = 0; q < kRelaxUnroll; ++q)
+        if (ok[q]) any_update |= relax_edge_seen<ALGO>(sv[q], dst[q], w[q], cur[q], a.value, a.nxt);
+    }
+  }
+  if (lane == 0 && (my_edges || my_srcs)) {
+    atomicAdd(&s_edges, my_edges);
+    atomicAdd(&s_srcs, my_srcs);
+  }
+  if (__syncthreads_or(any_update) && tid == 0) atomicAdd(&a.ctl->upd[slot], 1u);
+  if (tid == 0) {
+    if (s_edges) atomicAdd(&a.ctl->relaxed_edges, s_edges);
+    if (s_srcs) atomicAdd(&a.ctl->relaxed_sources, s_srcs);
+  }
+}
+
 // Chunk list of inner iteration `iter`: one warp per item.
 template <int ALGO, bool ASYNC, int W>
 __device__ __forceinline__ void relax_chunks_phase(const RelaxArgs &a) {

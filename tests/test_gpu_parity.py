@@ -228,10 +228,12 @@ def test_engine_matches_reference_golden(gpu):
 
 
 @pytest.mark.parametrize("mode", MODES)
-@pytest.mark.parametrize("flags", ["NO_PACK", "SCALAR_GATHER", "NO_PACK|SCALAR_GATHER"])
+@pytest.mark.parametrize("flags", ["NO_PACK", "SCALAR_GATHER", "NO_PACK|SCALAR_GATHER", "CTA_TILES",
+                                   "NO_PACK|CTA_TILES"])
 def test_transfer_forms(gpu, orc, g12w, mode, flags):
-    """8-byte records (SGW_OPT_NO_PACK) and the one-record-per-thread gather
-    (SGW_OPT_SCALAR_GATHER) give the same answers as the defaults."""
+    """8-byte records (SGW_OPT_NO_PACK), the one-record-per-thread gather
+    (SGW_OPT_SCALAR_GATHER) and CTA-tile expansion (SGW_OPT_CTA_TILES) give
+    the same answers as the defaults."""
     g = g12w
     f = 0
     for name in flags.split("|"):
