@@ -101,6 +101,11 @@ void sgw_graph_free(sgw_graph *g);
 /* Expand frontier edges in CTA tiles of 256 sources (k_relax_tile) instead
  * of warp tiles of 32 (k_relax_warp). */
 #define SGW_OPT_CTA_TILES 0x10u
+/* Weighted graphs whose weights do not pack beside the vertex id, but are
+ * all below 256, move as a u32 destination stream plus a u8 weight stream
+ * (5 bytes per edge; BFS/CC/PR move only the destinations).  This flag uses
+ * that split form even where the packed word would fit. */
+#define SGW_OPT_SPLIT_WEIGHTS 0x20u
 /* sched_flags: the learned policy's inner cap also covers compacted ranges */
 #define SGW_SCHED_CAP_COMPACT 0x1u
 /* sched_flags: transfer active vertices that cannot push, as the reference's

@@ -84,6 +84,14 @@ struct sgw_engine {
   Part *h_parts = nullptr;
   const uint32_t *d_host_edges = nullptr;  // device view of the transfer records
   const void *h_src = nullptr;             // host view of the transfer records
+  // Split form: weights below 256 that do not pack beside the vertex id
+  // travel as a separate byte stream (5 bytes per edge instead of 8).
+  bool split = false;
+  bool use_w = false;                      // this run reads the weight stream
+  const uint4 *d_host_w16 = nullptr;       // device view of the weight stream
+  const char *h_wsrc = nullptr;            // host view of the weight stream
+  uint8_t *d_wbuf[kMaxBuf] = {};           // weight bytes of each edge buffer
+  uint32_t rec_bytes = 4;                  // device bytes per edge in a buffer
   bool registered = false;
   uint32_t *h_packed = nullptr;            // packed transfer copy (weighted graphs)
   size_t packed_bytes = 0;
@@ -255,7 +263,7 @@ uint64_t fit_cap(int fam, const sgw_engine_opts &o, uint32_t n, uint32_t m, uint
 }
 
 int carve(sgw_engine *e, int fam, uint64_t cap) {
-  const Layout L = make_layout(fam, e->n, e->m, 4 * e->W, e->nbuf, e->num_tiles, cap,
+  const Layout L = make_layout(fam, e->n, e->m, e->rec_bytes, e->nbuf, e->num_tiles, cap,
                                e->opts.chunk_edges, e->opts.tile_degree_max);
   if (L.total > e->arena_bytes) return fail(SGW_EBUDGET, "layout exceeds the arena");
   char *b = e->d_arena;
@@ -278,7 +286,11 @@ int carve(sgw_engine *e, int fam, uint64_t cap) {
   e->d_mlp = (__nv_bfloat16 *)(b + L.mlp);
   e->d_sel_hist = (unsigned long long *)(b + L.sel);
   e->d_wl = (WorkItem *)(b + L.wl);
-  for (int i = 0; i < kMaxBuf; ++i) e->d_buf[i] = (uint32_t *)(b + L.buf[i]);
+  for (int i = 0; i < kMaxBuf; ++i) {
+    e->d_buf[i] = (uint32_t *)(b + L.buf[i]);
+    // split form: the buffer's cap weight bytes follow its cap end words
+    e->d_wbuf[i] = e->split ? (uint8_t *)(b + L.buf[i]) + 4ull * L.cap : nullptr;
+  }
   e->cap = L.cap;
   e->max_parts = L.max_parts;
   e->wl_cap = L.wl_cap;
@@ -329,8 +341,8 @@ uint32_t defer_permille(const sgw_engine *e) {
   const uint32_t o = e->opts.sched_defer_permille;
   if (o > 1000) return 0;
   if (o) return o;
-  const double edges = (double)e->m * 4.0 * e->W;
-  const double space = (double)e->nbuf * (double)e->cap * 4.0 * e->W;
+  const double edges = (double)e->m * e->rec_bytes;
+  const double space = (double)e->nbuf * (double)e->cap * e->rec_bytes;
   return edges > 4.0 * space ? 250u : 0u;
 }
 
@@ -451,7 +463,7 @@ void trace_partition(sgw_engine *e, uint32_t p, uint32_t inner) {
   r.active_edges = q.edge_count;
   r.iteration_active_nodes = e->num_active;
   r.iteration_active_edges = e->num_active_edges;
-  r.bytes_h2d = q.edge_count * 4ull * e->W;
+  r.bytes_h2d = q.edge_count * (4ull * e->W + (e->use_w ? 1 : 0));
   r.transfer = is_hub(e, q) ? 2 : 0;
   e->trace.push_back(r);
 }
@@ -474,10 +486,10 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
   const uint32_t grid = std::min<uint32_t>(grid_for(e, q.edge_count, kGatherTile), gmax);
   const uint4 *h16 = reinterpret_cast<const uint4 *>(e->d_host_edges);
   if (e->vec_gather && e->W == 1)
-    k_gather_v<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+    k_gather_v<4><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
                                                   q.from, q.size, q.edge_from, (uint32_t)q.edge_count);
   else if (e->vec_gather)
-    k_gather_v<2><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+    k_gather_v<8><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
                                                   q.from, q.size, q.edge_from, (uint32_t)q.edge_count);
   else if (e->W == 1)
     k_gather<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_edges,
@@ -488,9 +500,17 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
                                                 e->d_buf[b], q.from, q.size, q.edge_from,
                                                 (uint32_t)q.edge_count);
   CK(cudaGetLastError());
+  e->stats.h2d_bytes += q.edge_count * 4ull * e->W;
+  if (e->use_w) {  // the weight bytes of the same edges
+    k_gather_v<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_w16, e->d_wbuf[b],
+                                                  q.from, q.size, q.edge_from, (uint32_t)q.edge_count);
+    CK(cudaGetLastError());
+    e->stats.h2d_bytes += q.edge_count;
+    e->stats.launches += 1;
+    e->stats.gather_launches += 1;
+  }
   TRY(prof_end(e, s, slot));
   CK(cudaEventRecord(e->ev_ready[b], s));
-  e->stats.h2d_bytes += q.edge_count * 4ull * e->W;
   e->stats.launches += 1;
   e->stats.gather_launches += 1;
   return SGW_OK;
@@ -519,6 +539,7 @@ int launch_relax_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, u
   a.streamed = e->cur_streamed;
   a.stream_base = e->cur_stream_base;
   a.off = e->d_off;
+  a.wbuf = e->use_w ? e->d_wbuf[b] : nullptr;
   const uint32_t g1 = grid_for(e, q.size, kRelaxThreads);
   if (e->opts.flags & SGW_OPT_CTA_TILES) k_relax_tile<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
   else k_relax_warp<ALGO, ASYNC, W><<<g1, kRelaxThreads, 0, e->s_comp>>>(a);
@@ -595,8 +616,8 @@ int launch_relax(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, bool a
 
 template <int ALGO, int W>
 int launch_flat_w(sgw_engine *e, uint32_t b, uint32_t count) {
-  k_relax_flat<ALGO, W><<<grid_for(e, count, 256), 256, 0, e->s_comp>>>(e->d_buf[b], count, e->pbits,
-                                                                       e->d_value, e->d_l2, e->d_ctl);
+  k_relax_flat<ALGO, W><<<grid_for(e, count, 256), 256, 0, e->s_comp>>>(
+      e->d_buf[b], e->use_w ? e->d_wbuf[b] : nullptr, count, e->pbits, e->d_value, e->d_l2, e->d_ctl);
   CK(cudaGetLastError());
   return SGW_OK;
 }
@@ -624,8 +645,12 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
     TRY(prof_begin(e, K_GATHER, e->s_comp, &slot));
     CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->h_src + (hoff + s) * esz, cnt * esz,
                        cudaMemcpyHostToDevice, e->s_comp));
-    TRY(prof_end(e, e->s_comp, slot));
     e->stats.h2d_bytes += cnt * esz;
+    if (e->use_w) {
+      CK(cudaMemcpyAsync(e->d_wbuf[b], e->h_wsrc + hoff + s, cnt, cudaMemcpyHostToDevice, e->s_comp));
+      e->stats.h2d_bytes += cnt;
+    }
+    TRY(prof_end(e, e->s_comp, slot));
     TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
     int st = SGW_OK;
     switch (e->params.algo) {
@@ -708,6 +733,7 @@ int state_init(sgw_engine *e, const sgw_run_params *p) {
   TRY(validate_params(e, p));
   CK(cudaSetDevice(e->device));
   e->params = *p;
+  e->use_w = e->split && (p->algo == SGW_SSSP || p->algo == SGW_SSWP);
   e->stats = sgw_run_stats{};
   e->prof_used = 0;
   e->initialized = false;
@@ -822,6 +848,11 @@ int range_transfer(sgw_engine *e, Job &j, int b) {
     // relaxation running on the compute stream
     CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->h_src + (size_t)r.e0 * esz, bytes,
                        cudaMemcpyHostToDevice, e->s_copy));
+    if (e->use_w) {
+      CK(cudaMemcpyAsync(e->d_wbuf[b], e->h_wsrc + r.e0, (size_t)(r.e1 - r.e0), cudaMemcpyHostToDevice,
+                         e->s_copy));
+      e->stats.h2d_bytes += (size_t)(r.e1 - r.e0);
+    }
     TRY(prof_end(e, e->s_copy, slot));
     CK(cudaEventRecord(e->ev_ready[b], e->s_copy));
     e->stats.h2d_bytes += bytes;
@@ -838,7 +869,7 @@ int range_transfer(sgw_engine *e, Job &j, int b) {
 // All active ranges of one global iteration under the learned policy.
 int process_iteration_ranges(sgw_engine *e) {
   const uint32_t S = (uint32_t)e->ranges.size();
-  const uint32_t esz = 4 * e->W;
+  const uint32_t esz = 4 * e->W + (e->use_w ? 1 : 0);  // bytes moved per edge
   std::vector<int> held(S, -1);
   for (uint32_t b = 0; b < e->nbuf; ++b)
     if (e->buf_range[b] >= 0) held[e->buf_range[b]] = (int)b;
@@ -1118,9 +1149,14 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   e->m = g->m;
   e->W = g->weighted ? 2 : 1;
   // weighted records travel as one packed word when (w << bits(n)) | dst fits
-  bool pack = g->weighted && !(o.flags & SGW_OPT_NO_PACK) && pack_bits(g, &e->pbits);
+  bool pack = g->weighted && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SPLIT_WEIGHTS)) && pack_bits(g, &e->pbits);
   if (pack) e->W = 1;
   else e->pbits = 0;
+  // otherwise weights below 256 travel as their own byte stream
+  e->split = g->weighted && !pack && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SCALAR_GATHER)) &&
+             max_weight(g) < 256;
+  if (e->split) e->W = 1;
+  e->rec_bytes = 4 * e->W + (e->split ? 1 : 0);
   e->nbuf = (o.flags & SGW_OPT_NO_OVERLAP) ? 1 : 2;
   if (o.num_buffers) {
     if (o.num_buffers > (uint32_t)kMaxBuf) { delete e; return fail(SGW_EINVAL, "num_buffers above %d", kMaxBuf); }
@@ -1131,7 +1167,7 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   if (cudaGetDeviceProperties(&prop, o.device) != cudaSuccess) { delete e; return fail(SGW_ECUDA, "device properties"); }
   e->num_sms = prop.multiProcessorCount;
 
-  const uint32_t esz = 4 * e->W;
+  const uint32_t esz = e->rec_bytes;
   // The arena never exceeds what holds the whole graph in both buffers.
   const uint64_t mfull = std::max<uint64_t>(e->m, 64);
   size_t need = 0;
@@ -1181,7 +1217,9 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   // padding let the 16-byte vector reads run past the last record.
   if (g->m > 0) {
     const size_t rec_bytes = (size_t)e->m * 4 * e->W;
-    e->packed_bytes = (rec_bytes + 16 + 15) / 16 * 16;
+    const size_t ends_alloc = (rec_bytes + 16 + 15) / 16 * 16;
+    const size_t w_alloc = e->split ? ((size_t)e->m + 16 + 15) / 16 * 16 : 0;
+    e->packed_bytes = ends_alloc + w_alloc;
     ce = cudaHostAlloc((void **)&e->h_packed, e->packed_bytes, cudaHostAllocMapped | cudaHostAllocPortable);
     if (ce != cudaSuccess) {
       cudaGetLastError();
@@ -1190,14 +1228,19 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
                           cudaGetErrorString(ce)));
     }
     e->packed_registered = true;  // owned by the CUDA runtime: cudaFreeHost on destroy
+    char *hw = (char *)e->h_packed + ends_alloc;
     if (pack) pack_into(g, e->pbits, e->h_packed);
+    else if (e->split) split_into(g, e->h_packed, (uint8_t *)hw);
     else copy_records(g, e->h_packed);
-    memset((char *)e->h_packed + rec_bytes, 0, e->packed_bytes - rec_bytes);
+    memset((char *)e->h_packed + rec_bytes, 0, ends_alloc - rec_bytes);
+    if (e->split) memset(hw + e->m, 0, w_alloc - e->m);
     e->h_src = e->h_packed;
+    e->h_wsrc = e->split ? hw : nullptr;
     void *dp = nullptr;
     ce = cudaHostGetDevicePointer(&dp, e->h_packed, 0);
     if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce))); }
     e->d_host_edges = (const uint32_t *)dp;
+    if (e->split) e->d_host_w16 = reinterpret_cast<const uint4 *>((const char *)dp + ends_alloc);
   }
   e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && e->d_host_edges &&
                   ((uintptr_t)e->d_host_edges % 16 == 0);
@@ -1335,7 +1378,7 @@ int sgw_sched_buffers(const sgw_graph *g, uint64_t budget_bytes, uint32_t *num_b
   clear_error();
   if (!g || !num_buffers) return fail(SGW_EINVAL, "null argument");
   uint32_t bits = 0;
-  const double rec = g->weighted && !pack_bits(g, &bits) ? 8.0 : 4.0;
+  const double rec = !g->weighted || pack_bits(g, &bits) ? 4.0 : (max_weight(g) < 256 ? 5.0 : 8.0);
   const double space = (double)budget_bytes - 18.0 * (double)g->n;  // integer vertex state
   const double third = space > 0 ? space / 3.0 / rec : 0.0;
   *num_buffers = (g->m > 0 && third >= 0.15 * (double)g->m) ? 3u : 2u;

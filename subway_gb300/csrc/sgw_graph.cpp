@@ -100,6 +100,24 @@ void copy_records(const sgw_graph *g, void *out) {
   }
 }
 
+uint32_t max_weight(const sgw_graph *g) {
+  if (!g->weighted || g->m == 0) return 0;
+  const uint32_t *ed = (const uint32_t *)g->edges;
+  uint32_t wmax = 0;
+#pragma omp parallel for reduction(max : wmax)
+  for (int64_t i = 0; i < (int64_t)g->m; ++i) wmax = std::max(wmax, ed[2 * size_t(i) + 1]);
+  return wmax;
+}
+
+void split_into(const sgw_graph *g, uint32_t *ends, uint8_t *w8) {
+  const uint32_t *ed = (const uint32_t *)g->edges;
+#pragma omp parallel for
+  for (int64_t i = 0; i < (int64_t)g->m; ++i) {
+    ends[i] = ed[2 * size_t(i)];
+    w8[i] = (uint8_t)ed[2 * size_t(i) + 1];
+  }
+}
+
 bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint32_t *nbits) {
   *out = nullptr;
   uint32_t nb = 0;

@@ -583,17 +583,19 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(
 
 // Same tiling as k_gather, but host memory is read as aligned 16-byte words:
 // each source's clipped host range is covered by ceil-aligned chunks of
-// R = 4 / W records, the CTA scans the chunk counts of its tile's sources, and
-// every thread loads whole chunks (4 in flight) and scatters the records that
-// belong to the source into the device buffer.  Needs a 16-byte aligned host
-// array (the engine's own allocations are 64 KiB aligned).
-template <int W>
+// R = 16 / RB records of RB bytes, the CTA scans the chunk counts of its
+// tile's sources, and every thread loads whole chunks (4 in flight) and
+// scatters the records that belong to the source into the device buffer.
+// RB = 4 (one word per edge), 8 (the reference's {end, w8}) or 1 (the weight
+// stream of the split form).  Needs a 16-byte aligned host array (the
+// engine's own allocations are 64 KiB aligned).
+template <int RB>
 __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
     const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
     const uint32_t *__restrict__ off, const uint4 *__restrict__ host16,
-    uint32_t *__restrict__ buf, uint32_t from, uint32_t size, uint32_t edge_from,
+    void *__restrict__ buf, uint32_t from, uint32_t size, uint32_t edge_from,
     uint32_t edge_count) {
-  constexpr uint32_t R = 4 / W;  // records per 16-byte chunk
+  constexpr uint32_t R = 16 / RB;  // records per 16-byte chunk
   __shared__ uint32_t s_bpos[kGatherTile + 1];
   __shared__ uint32_t s_hlo[kGatherTile + 1];
   __shared__ uint32_t s_len[kGatherTile + 1];
@@ -691,8 +693,9 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
           const uint32_t rec = cc[u] * R + r;
           if (rec >= hlo && rec - hlo < len) {
             const uint32_t o = bpos + (rec - hlo);
-            if (W == 1) buf[o] = w[r];
-            else reinterpret_cast<uint2 *>(buf)[o] = make_uint2(w[2 * r], w[2 * r + 1]);
+            if (RB == 4) reinterpret_cast<uint32_t *>(buf)[o] = w[r];
+            else if (RB == 8) reinterpret_cast<uint2 *>(buf)[o] = make_uint2(w[2 * r], w[2 * r + 1]);
+            else reinterpret_cast<uint8_t *>(buf)[o] = (uint8_t)(w[r / 4] >> (8 * (r % 4)));
           }
         }
       }
@@ -761,15 +764,15 @@ __device__ __forceinline__ bool can_push(uint32_t v) {
 }
 
 // Reads edge record e of a device edge buffer: W = 2 words {end, w8};
-// W = 1 either an unweighted {end} (pbits = 0) or the packed transfer form
-// (w8 << pbits) | end.
+// W = 1 either {end} (pbits = 0; its weight, if any, in the byte stream wbuf
+// of the split form) or the packed transfer form (w8 << pbits) | end.
 template <int W>
 __device__ __forceinline__ void load_edge(const uint32_t *buf, uint32_t e, uint32_t pbits,
-                                          uint32_t &dst, uint32_t &w) {
+                                          uint32_t &dst, uint32_t &w, const uint8_t *wbuf = nullptr) {
   if (W == 1) {
     const uint32_t r = buf[e];
     if (pbits) { dst = r & ((1u << pbits) - 1u); w = r >> pbits; }
-    else { dst = r; w = 0; }
+    else { dst = r; w = wbuf ? (uint32_t)wbuf[e] : 0u; }
   } else {
     const uint2 ed = reinterpret_cast<const uint2 *>(buf)[e];
     dst = ed.x;
@@ -797,6 +800,7 @@ struct RelaxArgs {
   uint32_t streamed;
   uint32_t stream_base;
   const uint32_t *off;
+  const uint8_t *wbuf;       // split form: the buffer's weight bytes (else null)
 };
 
 constexpr int kRelaxThreads = 256;
@@ -936,7 +940,7 @@ __device__ __forceinline__ void relax_tile_phase(const RelaxArgs &a, TileSmem &s
             if (s_scan[mid] <= j) lo = mid + 1; else hi = mid;
           }
           const uint32_t k = lo - 1;
-          load_edge<W>(a.buf, s_boff[k] + (j - s_scan[k]), a.pbits, dst[q], w[q]);
+          load_edge<W>(a.buf, s_boff[k] + (j - s_scan[k]), a.pbits, dst[q], w[q], a.wbuf);
           sv[q] = s_val[k];
         }
       }
@@ -1067,7 +1071,7 @@ __global__ void __launch_bounds__(kRelaxThreads, 5) k_relax_warp(RelaxArgs a) {
             if (excl_s[mid] <= j) lo = mid + 1; else hi = mid;
           }
           const uint32_t k = lo - 1;
-          load_edge<W>(a.buf, boff_s[k] + (j - excl_s[k]), a.pbits, dst[q], w[q]);
+          load_edge<W>(a.buf, boff_s[k] + (j - excl_s[k]), a.pbits, dst[q], w[q], a.wbuf);
           sv[q] = val_s[k];
         }
       }
@@ -1106,7 +1110,7 @@ __device__ __forceinline__ void relax_chunks_phase(const RelaxArgs &a) {
       uint32_t dst[kRelaxUnroll], w[kRelaxUnroll], cur[kRelaxUnroll];
 #pragma unroll
       for (int q = 0; q < kRelaxUnroll; ++q)
-        if (j0 + 32 * q < wi.count) load_edge<W>(a.buf, wi.boff + j0 + 32 * q, a.pbits, dst[q], w[q]);
+        if (j0 + 32 * q < wi.count) load_edge<W>(a.buf, wi.boff + j0 + 32 * q, a.pbits, dst[q], w[q], a.wbuf);
 #pragma unroll
       for (int q = 0; q < kRelaxUnroll; ++q)
         if (j0 + 32 * q < wi.count) cur[q] = a.value[dst[q]];
@@ -1140,15 +1144,15 @@ __global__ void k_hub_claim(uint32_t u, const uint32_t *value, uint8_t *l1, uint
 }
 
 template <int ALGO, int W>
-__global__ void k_relax_flat(const uint32_t *buf, uint32_t count, uint32_t pbits, uint32_t *value,
-                             uint8_t *nxt, Ctl *ctl) {
+__global__ void k_relax_flat(const uint32_t *buf, const uint8_t *wbuf, uint32_t count, uint32_t pbits,
+                             uint32_t *value, uint8_t *nxt, Ctl *ctl) {
   if (!ctl->hub_active) return;
   const uint32_t sval = ctl->hub_value;
   if (!can_push<ALGO>(sval)) return;
   bool any = false;
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
     uint32_t dst, w;
-    load_edge<W>(buf, j, pbits, dst, w);
+    load_edge<W>(buf, j, pbits, dst, w, wbuf);
     any |= relax_edge<ALGO>(sval, dst, w, value, nxt);
   }
   if (__syncthreads_or(any) && threadIdx.x == 0) atomicAdd(&ctl->upd[1], 1u);

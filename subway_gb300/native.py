@@ -23,6 +23,7 @@ OPT_NO_OVERLAP = 0x2
 OPT_NO_PACK = 0x4
 OPT_SCALAR_GATHER = 0x8
 OPT_CTA_TILES = 0x10
+OPT_SPLIT_WEIGHTS = 0x20
 SCHED_CAP_COMPACT = 0x1
 SCHED_KEEP_IDLE = 0x2
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}

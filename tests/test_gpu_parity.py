@@ -229,7 +229,7 @@ def test_engine_matches_reference_golden(gpu):
 
 @pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("flags", ["NO_PACK", "SCALAR_GATHER", "NO_PACK|SCALAR_GATHER", "CTA_TILES",
-                                   "NO_PACK|CTA_TILES"])
+                                   "NO_PACK|CTA_TILES", "SPLIT_WEIGHTS", "SPLIT_WEIGHTS|CTA_TILES"])
 def test_transfer_forms(gpu, orc, g12w, mode, flags):
     """8-byte records (SGW_OPT_NO_PACK), the one-record-per-thread gather
     (SGW_OPT_SCALAR_GATHER) and CTA-tile expansion (SGW_OPT_CTA_TILES) give
@@ -257,6 +257,26 @@ def test_async_inner_cap(gpu, orc, g12w):
             assert np.array_equal(vals, _oracle(orc, g, algo, src)), (algo, mi)
             assert st["partitions"] >= st["global_iterations"] > 0
             assert st["inner_iterations"] <= mi * st["partitions"], (algo, mi)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_split_weights_bytes_and_answers(gpu, orc, g12w, mode):
+    """The split form moves 4 bytes per edge for BFS/CC and 5 for SSSP/SSWP
+    (destination word + weight byte), under plain and learned schedules,
+    with hub vertices streamed in pieces, and answers like the oracle."""
+    g = g12w
+    budget = 18 * g.n + 72 * 1024 + 1500 * 20
+    for policy in ("plain", "learned"):
+        eng = gpu.Engine(g, budget_bytes=budget, flags=gpu.OPT_SPLIT_WEIGHTS,
+                         num_buffers=3 if policy == "learned" else 0)
+        if policy == "learned":
+            eng.set_policy("learned")
+        src = int(g.pick_sources(1, seed=4)[0])
+        for algo in ALGS:
+            vals, st = eng.run(algo, mode, src)
+            assert np.array_equal(vals, _oracle(orc, g, algo, src)), (algo, mode, policy)
+            per_edge = 5 if algo in ("sssp", "sswp") else 4
+            assert st["h2d_bytes"] % per_edge == 0, (algo, st["h2d_bytes"])
 
 
 def test_wide_weights_fall_back_to_full_records(gpu, orc):
