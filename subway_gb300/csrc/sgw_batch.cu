@@ -49,21 +49,25 @@ struct BItem {
 
 // counters: [0] work items, [1] frontier vertices, [2] iterations run,
 // [3] error (1 = item list overflow, 2 = iteration limit)
-__global__ void k_b_fill(uint32_t *dist, size_t count, unsigned long long *next, uint32_t n) {
+__global__ void k_b_fill(uint32_t *dist, size_t count, unsigned long long *next, unsigned long long *seen,
+                         uint32_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
     dist[i] = kBInf;
-  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x)
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
     next[v] = 0ull;
+    seen[v] = 0ull;
+  }
 }
 
 template <int L>
 __global__ void k_b_seed(const uint32_t *src, uint32_t nsrc, uint32_t *dist, unsigned long long *next,
-                         uint32_t *ctr) {
+                         unsigned long long *seen, uint32_t *ctr) {
   const uint32_t l = threadIdx.x;
   if (l < nsrc) {
     const uint32_t s = src[l];
     dist[(size_t)s * L + l] = 0;
     atomicOr(&next[s], 1ull << l);
+    atomicOr(&seen[s], 1ull << l);
   }
   if (l == 0) { ctr[0] = 0; ctr[1] = 0; ctr[2] = 0; ctr[3] = 0; }
 }
@@ -187,6 +191,40 @@ __global__ void __launch_bounds__(kBThreads) k_b_relax(const BItem *__restrict__
   }
 }
 
+// BFS, bit-parallel over the lanes (multi-source BFS): a vertex's 64-bit
+// `seen` mask holds the queries that have reached it.  Lane k of the warp
+// takes edge c + k of the item; one atomicOr claims, for every query whose
+// frontier holds the item's vertex, the destination's still-unseen lanes;
+// those get level = iteration + 1 and join the next frontier.  Each (vertex,
+// query) bit is claimed exactly once, so the levels are the BFS levels.
+template <int W, int L>
+__global__ void __launch_bounds__(kBThreads) k_b_bfs_relax(const BItem *__restrict__ items, const uint32_t *ctr,
+                                                           uint32_t cap, const uint32_t *__restrict__ edges,
+                                                           uint32_t pbits, uint32_t *dist,
+                                                           const unsigned long long *__restrict__ cur,
+                                                           unsigned long long *next, unsigned long long *seen) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t nitems = min(ctr[0], cap);
+  const uint32_t level = ctr[2] + 1;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t dmask = pbits ? ((1u << pbits) - 1u) : 0xffffffffu;
+  for (uint32_t i = gw; i < nitems; i += nw) {
+    const BItem it = items[i];
+    const unsigned long long f = cur[it.u];
+    if (f == 0ull) continue;
+    for (uint32_t c = lane; c < it.cnt; c += 32) {
+      const size_t e = (size_t)it.e0 + c;
+      const uint32_t dst = W == 1 ? (edges[e] & dmask) : edges[2 * e];
+      if ((seen[dst] & f) == f) continue;  // every query here has been there (a stale read only costs the atomic)
+      const unsigned long long fresh = f & ~atomicOr(&seen[dst], f);
+      if (fresh == 0ull) continue;
+      atomicOr(&next[dst], fresh);
+      for (unsigned long long m = fresh; m; m &= m - 1) dist[(size_t)dst * L + (__ffsll((long long)m) - 1)] = level;
+    }
+  }
+}
+
 __global__ void k_b_cond(cudaGraphConditionalHandle handle, uint32_t *ctr, uint32_t max_iters) {
   const uint32_t it = ++ctr[2];
   uint32_t go = ctr[1] > 0 ? 1u : 0u;
@@ -224,7 +262,7 @@ struct sgw_batch {
   char *d_arena = nullptr;
   size_t arena_bytes = 0;
   uint32_t *d_off = nullptr, *d_edges = nullptr, *d_dist = nullptr, *d_stage = nullptr;
-  unsigned long long *d_cur = nullptr, *d_next = nullptr;
+  unsigned long long *d_cur = nullptr, *d_next = nullptr, *d_seen = nullptr;
   BItem *d_items = nullptr;
   uint32_t *d_ctr = nullptr, *d_src = nullptr;
   uint32_t stage_vertices = 0;
@@ -248,8 +286,12 @@ int capture_body(sgw_batch *b, cudaGraph_t body, cudaGraphConditionalHandle h) {
   const uint32_t grid = (uint32_t)b->num_sms * 8;
   k_b_frontier<<<grid, kBThreads, 0, b->s>>>(b->n, b->d_off, b->d_cur, b->d_next, b->d_items, b->items_cap,
                                              b->d_ctr, b->chunk);
-  k_b_relax<SSSP, W, L><<<grid, kBThreads, 0, b->s>>>(b->d_items, b->d_ctr, b->items_cap, b->d_edges, b->pbits,
-                                                      b->d_dist, b->d_cur, b->d_next);
+  if (SSSP)
+    k_b_relax<SSSP, W, L><<<grid, kBThreads, 0, b->s>>>(b->d_items, b->d_ctr, b->items_cap, b->d_edges, b->pbits,
+                                                        b->d_dist, b->d_cur, b->d_next);
+  else
+    k_b_bfs_relax<W, L><<<grid, kBThreads, 0, b->s>>>(b->d_items, b->d_ctr, b->items_cap, b->d_edges, b->pbits,
+                                                      b->d_dist, b->d_cur, b->d_next, b->d_seen);
   k_b_cond<<<1, 1, 0, b->s>>>(h, b->d_ctr, b->max_iters);
   cudaGraph_t out = nullptr;
   CK(cudaStreamEndCapture(b->s, &out));
@@ -324,7 +366,7 @@ int sgw_batch_create(const sgw_graph *g, const sgw_engine_opts *opts, uint32_t l
   b->items_cap = (uint32_t)std::min<uint64_t>((uint64_t)g->m / b->chunk + g->n + 64, 0xffffffffull);
   b->stage_vertices = std::min<uint32_t>(g->n, 1u << 22);
   const size_t need = al(4ull * (g->n + 1)) + al((size_t)g->m * 4 * b->W) + al((size_t)g->n * lanes * 4) +
-                      2 * al(8ull * g->n) + al(sizeof(BItem) * (size_t)b->items_cap) + al(64) + al(256) +
+                      3 * al(8ull * g->n) + al(sizeof(BItem) * (size_t)b->items_cap) + al(64) + al(256) +
                       al((size_t)b->stage_vertices * lanes * 4);
   if (o.budget_bytes && need > o.budget_bytes) {
     sgw::host_free(packed);
@@ -342,6 +384,7 @@ int sgw_batch_create(const sgw_graph *g, const sgw_engine_opts *opts, uint32_t l
   b->d_dist = (uint32_t *)take((size_t)g->n * lanes * 4);
   b->d_cur = (unsigned long long *)take(8ull * g->n);
   b->d_next = (unsigned long long *)take(8ull * g->n);
+  b->d_seen = (unsigned long long *)take(8ull * g->n);
   b->d_items = (BItem *)take(sizeof(BItem) * (size_t)b->items_cap);
   b->d_ctr = (uint32_t *)take(64);
   b->d_src = (uint32_t *)take(256);
@@ -412,9 +455,9 @@ int sgw_batch_run(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc
   CK(cudaMemcpyAsync(b->d_src, sources, 4ull * nsrc, cudaMemcpyHostToDevice, b->s));
   CK(cudaEventRecord(b->t0, b->s));
   const size_t cells = (size_t)b->n * b->lanes;
-  k_b_fill<<<b->num_sms * 8, 256, 0, b->s>>>(b->d_dist, cells, b->d_next, b->n);
-  if (b->lanes == 64) k_b_seed<64><<<1, 64, 0, b->s>>>(b->d_src, nsrc, b->d_dist, b->d_next, b->d_ctr);
-  else k_b_seed<32><<<1, 64, 0, b->s>>>(b->d_src, nsrc, b->d_dist, b->d_next, b->d_ctr);
+  k_b_fill<<<b->num_sms * 8, 256, 0, b->s>>>(b->d_dist, cells, b->d_next, b->d_seen, b->n);
+  if (b->lanes == 64) k_b_seed<64><<<1, 64, 0, b->s>>>(b->d_src, nsrc, b->d_dist, b->d_next, b->d_seen, b->d_ctr);
+  else k_b_seed<32><<<1, 64, 0, b->s>>>(b->d_src, nsrc, b->d_dist, b->d_next, b->d_seen, b->d_ctr);
   CK(cudaGetLastError());
   CK(cudaGraphLaunch(b->exec[algo == SGW_SSSP ? 1 : 0], b->s));
   CK(cudaEventRecord(b->t1, b->s));

@@ -485,12 +485,18 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
   const uint32_t gmax = e->opts.gather_ctas ? e->opts.gather_ctas : 2u * e->num_sms;
   const uint32_t grid = std::min<uint32_t>(grid_for(e, q.edge_count, kGatherTile), gmax);
   const uint4 *h16 = reinterpret_cast<const uint4 *>(e->d_host_edges);
-  if (e->vec_gather && e->W == 1)
-    k_gather_v<4><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
-                                                  q.from, q.size, q.edge_from, (uint32_t)q.edge_count);
+  if (e->vec_gather && e->W == 1 && e->use_w)  // split form: destination words and weight bytes
+    k_gather_v<4, true><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+                                                        e->d_host_w16, e->d_wbuf[b], q.from, q.size,
+                                                        q.edge_from, (uint32_t)q.edge_count);
+  else if (e->vec_gather && e->W == 1)
+    k_gather_v<4, false><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+                                                         nullptr, nullptr, q.from, q.size, q.edge_from,
+                                                         (uint32_t)q.edge_count);
   else if (e->vec_gather)
-    k_gather_v<8><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
-                                                  q.from, q.size, q.edge_from, (uint32_t)q.edge_count);
+    k_gather_v<8, false><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+                                                         nullptr, nullptr, q.from, q.size, q.edge_from,
+                                                         (uint32_t)q.edge_count);
   else if (e->W == 1)
     k_gather<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_edges,
                                                 e->d_buf[b], q.from, q.size, q.edge_from,
@@ -500,15 +506,7 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
                                                 e->d_buf[b], q.from, q.size, q.edge_from,
                                                 (uint32_t)q.edge_count);
   CK(cudaGetLastError());
-  e->stats.h2d_bytes += q.edge_count * 4ull * e->W;
-  if (e->use_w) {  // the weight bytes of the same edges
-    k_gather_v<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_w16, e->d_wbuf[b],
-                                                  q.from, q.size, q.edge_from, (uint32_t)q.edge_count);
-    CK(cudaGetLastError());
-    e->stats.h2d_bytes += q.edge_count;
-    e->stats.launches += 1;
-    e->stats.gather_launches += 1;
-  }
+  e->stats.h2d_bytes += q.edge_count * (4ull * e->W + (e->use_w ? 1 : 0));
   TRY(prof_end(e, s, slot));
   CK(cudaEventRecord(e->ev_ready[b], s));
   e->stats.launches += 1;
@@ -1185,8 +1183,12 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
     budget = (uint64_t)(state + std::max(0.0, edges_bytes));
   }
   const size_t arena = (size_t)std::min<uint64_t>(budget, need);
-  for (int fam = 0; fam < 2; ++fam)
+  for (int fam = 0; fam < 2; ++fam) {
     e->cap_fam[fam] = fit_cap(fam, o, e->n, e->m, esz, e->nbuf, e->num_tiles, arena);
+    // split form: the weight bytes start at 4 * cap past a 256-byte aligned
+    // buffer; a multiple of 4 keeps them 16-byte aligned for vector stores
+    if (e->split && e->cap_fam[fam] > 16) e->cap_fam[fam] &= ~3ull;
+  }
   if (e->cap_fam[FAM_INT] == 0) {
     const Layout L0 = make_layout(FAM_INT, e->n, e->m, esz, e->nbuf, e->num_tiles, 4096,
                                   o.chunk_edges, o.tile_degree_max);

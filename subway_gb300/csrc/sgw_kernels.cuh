@@ -586,16 +586,101 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(
 // R = 16 / RB records of RB bytes, the CTA scans the chunk counts of its
 // tile's sources, and every thread loads whole chunks (4 in flight) and
 // scatters the records that belong to the source into the device buffer.
-// RB = 4 (one word per edge), 8 (the reference's {end, w8}) or 1 (the weight
-// stream of the split form).  Needs a 16-byte aligned host array (the
-// engine's own allocations are 64 KiB aligned).
+// RB = 4 (one word per edge) or 8 (the reference's {end, w8}).  With WS the
+// split form's weight bytes of the same edges follow in the same tile (same
+// source ranges, chunks of 16 weights), put together in shared memory and
+// stored as 16-byte words.  Needs 16-byte aligned host arrays (the engine's
+// own allocations are 64 KiB aligned).
+constexpr uint32_t kGatherPer = (kGatherTile + kGatherThreads - 1) / kGatherThreads;
+
+// Exclusive scan of the tile's per-source chunk counts (R records per
+// chunk) into s_cs; returns the tile's chunk total.
+template <uint32_t R>
+__device__ __forceinline__ uint32_t gather_scan(uint32_t nsrc, const uint32_t *s_hlo, const uint32_t *s_len,
+                                                uint32_t *s_cs, uint32_t *s_part) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t cnt[kGatherPer];
+  uint32_t part = 0;
+#pragma unroll
+  for (uint32_t q = 0; q < kGatherPer; ++q) {
+    const uint32_t k = tid * kGatherPer + q;
+    cnt[q] = 0;
+    if (k < nsrc) {
+      const uint32_t hlo = s_hlo[k], len = s_len[k];
+      cnt[q] = (hlo + len + R - 1) / R - hlo / R;
+      part += cnt[q];
+    }
+  }
+  const uint32_t incl = warp_incl_scan(part, lane);
+  if (lane == 31) s_part[warp] = incl;
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t acc = 0;
+    for (int w = 0; w < kGatherThreads / 32; ++w) { uint32_t x = s_part[w]; s_part[w] = acc; acc += x; }
+    s_part[kGatherThreads] = acc;
+  }
+  __syncthreads();
+  uint32_t run = s_part[warp] + incl - part;
+#pragma unroll
+  for (uint32_t q = 0; q < kGatherPer; ++q) {
+    const uint32_t k = tid * kGatherPer + q;
+    if (k < nsrc) { s_cs[k] = run; run += cnt[q]; }
+  }
+  __syncthreads();
+  return s_part[kGatherThreads];
+}
+
+// Copies the tile's chunks of RB-byte records: RB 4 / 8 straight into buf,
+// RB 1 into the shared byte tile at position - j0.
 template <int RB>
+__device__ __forceinline__ void gather_copy(uint32_t total, uint32_t nsrc, uint32_t j0, const uint32_t *s_cs,
+                                            const uint32_t *s_hlo, const uint32_t *s_len, const uint32_t *s_bpos,
+                                            const uint4 *__restrict__ host16, void *__restrict__ buf,
+                                            uint8_t *s_bytes) {
+  constexpr uint32_t R = 16 / RB;
+  constexpr int U = 4;
+  for (uint32_t jb = threadIdx.x; jb < total; jb += U * blockDim.x) {
+    uint4 v[U];
+    uint32_t kk[U], cc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const uint32_t j = jb + u * blockDim.x;
+      kk[u] = 0xffffffffu;
+      if (j < total) {
+        const uint32_t k = last_le(s_cs, nsrc, j);
+        const uint32_t c = s_hlo[k] / R + (j - s_cs[k]);
+        kk[u] = k;
+        cc[u] = c;
+        v[u] = host16[c];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (kk[u] == 0xffffffffu) continue;
+      const uint32_t k = kk[u];
+      const uint32_t hlo = s_hlo[k], len = s_len[k], bpos = s_bpos[k];
+      const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+      for (uint32_t r = 0; r < R; ++r) {
+        const uint32_t rec = cc[u] * R + r;
+        if (rec >= hlo && rec - hlo < len) {
+          const uint32_t o = bpos + (rec - hlo);
+          if (RB == 4) reinterpret_cast<uint32_t *>(buf)[o] = w[r];
+          else if (RB == 8) reinterpret_cast<uint2 *>(buf)[o] = make_uint2(w[2 * r], w[2 * r + 1]);
+          else s_bytes[o - j0] = (uint8_t)(w[r / 4] >> (8 * (r % 4)));
+        }
+      }
+    }
+  }
+}
+
+template <int RB, bool WS>
 __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
     const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
     const uint32_t *__restrict__ off, const uint4 *__restrict__ host16,
-    void *__restrict__ buf, uint32_t from, uint32_t size, uint32_t edge_from,
-    uint32_t edge_count) {
-  constexpr uint32_t R = 16 / RB;  // records per 16-byte chunk
+    void *__restrict__ buf, const uint4 *__restrict__ host_w16, uint8_t *__restrict__ wbuf,
+    uint32_t from, uint32_t size, uint32_t edge_from, uint32_t edge_count) {
+  __shared__ __align__(16) uint8_t s_bytes[WS ? kGatherTile : 16];
   __shared__ uint32_t s_bpos[kGatherTile + 1];
   __shared__ uint32_t s_hlo[kGatherTile + 1];
   __shared__ uint32_t s_len[kGatherTile + 1];
@@ -625,79 +710,35 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
     }
     __syncthreads();
     const uint32_t first = s_first, nsrc = s_nsrc;
-    // per-source clipped ranges and chunk counts; each thread owns 8 sources
-    constexpr uint32_t PER = (kGatherTile + kGatherThreads - 1) / kGatherThreads;
-    uint32_t cnt[PER];
-    uint32_t part = 0;
+    // per-source clipped ranges (buffer position, host record, length)
 #pragma unroll
-    for (uint32_t q = 0; q < PER; ++q) {
-      const uint32_t k = tid * PER + q;
-      cnt[q] = 0;
+    for (uint32_t q = 0; q < kGatherPer; ++q) {
+      const uint32_t k = tid * kGatherPer + q;
       if (k < nsrc) {
         const uint32_t i = first + k;
         const uint32_t bp = ptr[i] - edge_from, be = ptr[i + 1] - edge_from;
         const uint32_t lo = max(bp, j0), hi = min(be, j1);
-        const uint32_t hlo = off[queue[i]] + (lo - bp);
         s_bpos[k] = lo;
-        s_hlo[k] = hlo;
+        s_hlo[k] = off[queue[i]] + (lo - bp);
         s_len[k] = hi - lo;
-        cnt[q] = (hlo + (hi - lo) + R - 1) / R - hlo / R;
-        part += cnt[q];
-      }
-    }
-    // block scan of the per-thread partial sums
-    {
-      const int lane = tid & 31, warp = tid >> 5;
-      const uint32_t incl = warp_incl_scan(part, lane);
-      if (lane == 31) s_part[warp] = incl;
-      __syncthreads();
-      if (tid == 0) {
-        uint32_t acc = 0;
-        for (int w = 0; w < kGatherThreads / 32; ++w) { uint32_t x = s_part[w]; s_part[w] = acc; acc += x; }
-        s_part[kGatherThreads] = acc;
-      }
-      __syncthreads();
-      uint32_t run = s_part[warp] + incl - part;
-#pragma unroll
-      for (uint32_t q = 0; q < PER; ++q) {
-        const uint32_t k = tid * PER + q;
-        if (k < nsrc) { s_cs[k] = run; run += cnt[q]; }
       }
     }
     __syncthreads();
-    const uint32_t total = s_part[kGatherThreads];
-    constexpr int U = 4;
-    for (uint32_t jb = tid; jb < total; jb += U * blockDim.x) {
-      uint4 v[U];
-      uint32_t kk[U], cc[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const uint32_t j = jb + u * blockDim.x;
-        kk[u] = 0xffffffffu;
-        if (j < total) {
-          const uint32_t k = last_le(s_cs, nsrc, j);
-          const uint32_t c = s_hlo[k] / R + (j - s_cs[k]);
-          kk[u] = k;
-          cc[u] = c;
-          v[u] = host16[c];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (kk[u] == 0xffffffffu) continue;
-        const uint32_t k = kk[u];
-        const uint32_t hlo = s_hlo[k], len = s_len[k], bpos = s_bpos[k];
-        const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-#pragma unroll
-        for (uint32_t r = 0; r < R; ++r) {
-          const uint32_t rec = cc[u] * R + r;
-          if (rec >= hlo && rec - hlo < len) {
-            const uint32_t o = bpos + (rec - hlo);
-            if (RB == 4) reinterpret_cast<uint32_t *>(buf)[o] = w[r];
-            else if (RB == 8) reinterpret_cast<uint2 *>(buf)[o] = make_uint2(w[2 * r], w[2 * r + 1]);
-            else reinterpret_cast<uint8_t *>(buf)[o] = (uint8_t)(w[r / 4] >> (8 * (r % 4)));
-          }
-        }
+    uint32_t total = gather_scan<16 / RB>(nsrc, s_hlo, s_len, s_cs, s_part);
+    gather_copy<RB>(total, nsrc, j0, s_cs, s_hlo, s_len, s_bpos, host16, buf, s_bytes);
+    if (WS) {
+      __syncthreads();  // s_cs is reused
+      total = gather_scan<16>(nsrc, s_hlo, s_len, s_cs, s_part);
+      gather_copy<1>(total, nsrc, j0, s_cs, s_hlo, s_len, s_bpos, host_w16, nullptr, s_bytes);
+      __syncthreads();
+      uint8_t *dst = wbuf + j0;
+      const uint32_t len = j1 - j0;
+      if (((uintptr_t)dst & 15u) == 0) {  // j0 is a multiple of the tile; wbuf is 16-byte aligned
+        for (uint32_t i = tid; i < len / 16u; i += blockDim.x)
+          reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(s_bytes)[i];
+        for (uint32_t i = (len & ~15u) + tid; i < len; i += blockDim.x) dst[i] = s_bytes[i];
+      } else {
+        for (uint32_t i = tid; i < len; i += blockDim.x) dst[i] = s_bytes[i];
       }
     }
     __syncthreads();
