@@ -599,17 +599,14 @@ template <uint32_t R>
 __device__ __forceinline__ uint32_t gather_scan(uint32_t nsrc, const uint32_t *s_hlo, const uint32_t *s_len,
                                                 uint32_t *s_cs, uint32_t *s_part) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  uint32_t cnt[kGatherPer];
+  auto chunks = [&](uint32_t k) {
+    const uint32_t hlo = s_hlo[k], len = s_len[k];
+    return (hlo + len + R - 1) / R - hlo / R;
+  };
   uint32_t part = 0;
-#pragma unroll
   for (uint32_t q = 0; q < kGatherPer; ++q) {
     const uint32_t k = tid * kGatherPer + q;
-    cnt[q] = 0;
-    if (k < nsrc) {
-      const uint32_t hlo = s_hlo[k], len = s_len[k];
-      cnt[q] = (hlo + len + R - 1) / R - hlo / R;
-      part += cnt[q];
-    }
+    if (k < nsrc) part += chunks(k);
   }
   const uint32_t incl = warp_incl_scan(part, lane);
   if (lane == 31) s_part[warp] = incl;
@@ -621,10 +618,9 @@ __device__ __forceinline__ uint32_t gather_scan(uint32_t nsrc, const uint32_t *s
   }
   __syncthreads();
   uint32_t run = s_part[warp] + incl - part;
-#pragma unroll
   for (uint32_t q = 0; q < kGatherPer; ++q) {
     const uint32_t k = tid * kGatherPer + q;
-    if (k < nsrc) { s_cs[k] = run; run += cnt[q]; }
+    if (k < nsrc) { s_cs[k] = run; run += chunks(k); }
   }
   __syncthreads();
   return s_part[kGatherThreads];
