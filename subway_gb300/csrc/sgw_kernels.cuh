@@ -1002,8 +1002,9 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
 // Warp-tile form of k_relax_tile: each warp takes 32 partition sources at a
 // time and expands their edges on its own (warp scan of the degrees, owner
 // found by binary search in the warp's slice of shared memory), so warps
-// never wait on each other inside the loop; the CTA meets once at the end to
-// publish its counters.  Sources above tile_degree_max go to the chunk list
+// never wait on each other: a warp that runs out of tiles adds its counters
+// to the CTA's in shared memory and leaves, and the last warp of the CTA to
+// leave publishes them.  Sources above tile_degree_max go to the chunk list
 // as in the CTA form.
 constexpr int kWarpsPerCta = kRelaxThreads / 32;
 template <int ALGO, bool ASYNC, int W>
@@ -1013,6 +1014,7 @@ __global__ void __launch_bounds__(kRelaxThreads, 5) k_relax_warp(RelaxArgs a) {
   __shared__ uint32_t s_val[kWarpsPerCta][32];
   __shared__ int s_skip;
   __shared__ unsigned long long s_edges, s_srcs;
+  __shared__ uint32_t s_any, s_done;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const uint32_t slot = a.iter & 3u;
   if (tid == 0) {
@@ -1021,6 +1023,8 @@ __global__ void __launch_bounds__(kRelaxThreads, 5) k_relax_warp(RelaxArgs a) {
     s_skip = skip;
     s_edges = 0;
     s_srcs = 0;
+    s_any = 0;
+    s_done = 0;
     if (blockIdx.x == 0) {
       a.ctl->upd[(a.iter + 1) & 3u] = 0;
       a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
@@ -1120,14 +1124,18 @@ __global__ void __launch_bounds__(kRelaxThreads, 5) k_relax_warp(RelaxArgs a) {
         if (ok[q]) any_update |= relax_edge_seen<ALGO>(sv[q], dst[q], w[q], cur[q], a.value, a.nxt);
     }
   }
-  if (lane == 0 && (my_edges || my_srcs)) {
-    atomicAdd(&s_edges, my_edges);
-    atomicAdd(&s_srcs, my_srcs);
-  }
-  if (__syncthreads_or(any_update) && tid == 0) atomicAdd(&a.ctl->upd[slot], 1u);
-  if (tid == 0) {
-    if (s_edges) atomicAdd(&a.ctl->relaxed_edges, s_edges);
-    if (s_srcs) atomicAdd(&a.ctl->relaxed_sources, s_srcs);
+  const bool warp_any = __any_sync(0xffffffffu, any_update);
+  if (lane == 0) {
+    if (my_edges) atomicAdd(&s_edges, my_edges);
+    if (my_srcs) atomicAdd(&s_srcs, my_srcs);
+    if (warp_any) atomicOr(&s_any, 1u);
+    __threadfence_block();
+    if (atomicAdd(&s_done, 1u) == kWarpsPerCta - 1) {  // the CTA's last warp publishes
+      __threadfence_block();
+      if (s_any) atomicAdd(&a.ctl->upd[slot], 1u);
+      if (s_edges) atomicAdd(&a.ctl->relaxed_edges, s_edges);
+      if (s_srcs) atomicAdd(&a.ctl->relaxed_sources, s_srcs);
+    }
   }
 }
 
