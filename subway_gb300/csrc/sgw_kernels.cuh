@@ -1008,7 +1008,7 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
 // as in the CTA form.
 constexpr int kWarpsPerCta = kRelaxThreads / 32;
 template <int ALGO, bool ASYNC, int W>
-__global__ void __launch_bounds__(kRelaxThreads, 5) k_relax_warp(RelaxArgs a) {
+__global__ void __launch_bounds__(kRelaxThreads, 4) k_relax_warp(RelaxArgs a) {
   __shared__ uint32_t s_excl[kWarpsPerCta][33];
   __shared__ uint32_t s_boff[kWarpsPerCta][32];
   __shared__ uint32_t s_val[kWarpsPerCta][32];
