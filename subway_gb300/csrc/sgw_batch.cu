@@ -176,11 +176,16 @@ __global__ void __launch_bounds__(kBThreads) k_b_relax(const BItem *__restrict__
 #pragma unroll
           for (int q = 0; q < kBUnroll; ++q) {
             if (k0 + q >= cnt) break;  // uniform across the warp
+            // a candidate below the value read improves the destination in
+            // this iteration (by this lane or by whichever wins), so the
+            // non-returning atomic suffices and the lane bit is right
             bool improved = false;
             if (active) {
               const uint32_t cand = du + (SSSP ? w[q] : 1u);
-              if (cand < seen[q])
-                improved = cand < atomicMin(&dist[(size_t)dst[q] * L + 32 * h + lane], cand);
+              if (cand < seen[q]) {
+                atomicMin(&dist[(size_t)dst[q] * L + 32 * h + lane], cand);
+                improved = true;
+              }
             }
             const uint32_t imp = __ballot_sync(0xffffffffu, improved);
             if (imp && lane == 0) atomicOr(&next[dst[q]], (unsigned long long)imp << (32 * h));

@@ -762,19 +762,23 @@ template <> struct Op<SGW_CC> {    // cc_kernel: value, atomicMin (:96-98)
   __device__ static uint32_t cand(uint32_t v, uint32_t) { return v; }
 };
 
-// Relaxes one edge given the destination's value as read beforehand (a
-// stale read only costs an extra atomic: values move one way); returns true
-// if the destination improved.
+// Relaxes one edge given the destination's value as read beforehand: when
+// the candidate beats it, a non-returning atomicMin/atomicMax (a reduction,
+// no round trip for the thread) lowers the value and the destination's label
+// is set.  The label is right even when another thread's candidate won: the
+// read value is at most as good as the value when this kernel started (values
+// move one way), so the candidate beat that value and the destination did
+// improve in this kernel, by this thread or by the winner.  Returns whether
+// the candidate beat the read value.
 template <int ALGO>
 __device__ __forceinline__ bool relax_edge_seen(uint32_t sval, uint32_t dst, uint32_t w, uint32_t cur,
                                                 uint32_t *value, uint8_t *nxt) {
   const uint32_t c = Op<ALGO>::cand(sval, w);
   if (Op<ALGO>::kMax ? (c > cur) : (c < cur)) {
-    const uint32_t old = Op<ALGO>::kMax ? atomicMax(&value[dst], c) : atomicMin(&value[dst], c);
-    if (Op<ALGO>::kMax ? (c > old) : (c < old)) {
-      nxt[dst] = 1;
-      return true;
-    }
+    if (Op<ALGO>::kMax) atomicMax(&value[dst], c);
+    else atomicMin(&value[dst], c);
+    nxt[dst] = 1;
+    return true;
   }
   return false;
 }
