@@ -61,6 +61,7 @@ struct sgw_engine {
   uint32_t *d_value = nullptr;
   uint8_t *d_l1 = nullptr, *d_l2 = nullptr;
   uint32_t range_inner_cap = 0;  // learned policy: inner-iteration cap of the running range
+  uint64_t hub_iters = 0;        // single-vertex partitions relaxed (counted on the host)
   uint32_t *d_queue = nullptr, *d_ptr = nullptr;
   uint32_t *d_tflag = nullptr;
   unsigned long long *d_tagg = nullptr, *d_tincl = nullptr;
@@ -181,6 +182,7 @@ int read_ctl(sgw_engine *e) {
   CK(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
   e->stats.d2h_bytes += sizeof(Ctl);
   CK(cudaStreamSynchronize(e->s_comp));
+  e->stats.inner_iterations = (uint64_t)e->h_ctl->iters_total + e->hub_iters;
   return check_ctl_error(e);
 }
 
@@ -407,7 +409,7 @@ int launch_generate(sgw_engine *e, int consume) {
   size_t slot = 0;
   TRY(prof_begin(e, K_GENERATE, e->s_comp, &slot));
   if (e->fam == FAM_PR) k_generate<true><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
-  else k_generate<false><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  else k_generate_v<<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
   CK(cudaGetLastError());
   TRY(prof_end(e, e->s_comp, slot));
   e->stats.launches += 1;
@@ -667,13 +669,19 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
     e->stats.launches += 1;
     e->stats.relax_launches += 1;
   }
+  e->hub_iters += 1;
   e->stats.inner_iterations += 1;
   return SGW_OK;
 }
 
 // Relaxation of one resident partition: sync = one pass; async = mixLabels
 // then inner iterations until no relaxation improves (or max_inner).
-int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_out) {
+// Inner iterations are counted on the device (Ctl::iters_total, refreshed
+// into the statistics by every control-block read); with sync_always false a
+// partition whose inner cap is reached returns without waiting for it, so
+// the host goes on enqueueing the next partition's work (*iters_out is then
+// 0: unknown until the next read).
+int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_out, bool sync_always = true) {
   const bool async = e->params.mode == SGW_ASYNC;
   // upd, wl_count, iters_run
   CK(cudaMemsetAsync(&e->d_ctl->upd[0], 0, sizeof(uint32_t) * 9, e->s_comp));
@@ -682,7 +690,6 @@ int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_o
     TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
     TRY(launch_relax(e, q, b, 1, false));
     TRY(prof_end(e, e->s_comp, slot));
-    e->stats.inner_iterations += 1;
     if (iters_out) *iters_out = 1;
     return SGW_OK;
   }
@@ -701,14 +708,16 @@ int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_o
     TRY(prof_begin(e, K_RELAX, e->s_comp, &slot));
     for (uint32_t k = 0; k < nb; ++k, ++iter) TRY(launch_relax(e, q, b, iter, true));
     TRY(prof_end(e, e->s_comp, slot));
-    TRY(read_ctl(e));
     const uint32_t last = iter - 1;
+    if (!sync_always && last >= max_inner) {  // capped: nothing to decide on the host
+      if (iters_out) *iters_out = 0;
+      return SGW_OK;
+    }
+    TRY(read_ctl(e));
     if (e->h_ctl->upd[last & 3u] == 0) break;  // converged
     if (last >= max_inner) break;             // leftover labels go to the next generate
   }
-  const uint32_t ran = e->h_ctl->iters_run;
-  e->stats.inner_iterations += ran;
-  if (iters_out) *iters_out = ran;
+  if (iters_out) *iters_out = e->h_ctl->iters_run;
   return SGW_OK;
 }
 
@@ -733,6 +742,7 @@ int state_init(sgw_engine *e, const sgw_run_params *p) {
   e->params = *p;
   e->use_w = e->split && (p->algo == SGW_SSSP || p->algo == SGW_SSWP);
   e->stats = sgw_run_stats{};
+  e->hub_iters = 0;
   e->prof_used = 0;
   e->initialized = false;
   e->gitr = 0;
@@ -993,7 +1003,7 @@ int process_iteration_ranges(sgw_engine *e) {
       for (uint32_t s = j.s; s < j.s_end; ++s) pred = std::max(pred, e->h_rstat[s].pred);
       const bool cappable = kept || (e->opts.sched_flags & SGW_SCHED_CAP_COMPACT);
       e->range_inner_cap = cappable && (double)pred >= thr ? (e->opts.sched_inner ? e->opts.sched_inner : 2u) : 0u;
-      const int st = process_resident(e, q, (uint32_t)j.buf, &inner);
+      const int st = process_resident(e, q, (uint32_t)j.buf, &inner, e->trace_on);
       e->cur_streamed = 0;
       e->range_inner_cap = 0;
       TRY(st);
@@ -1535,6 +1545,7 @@ int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values, sgw_run_st
   e->stats.reached_edges = pr ? e->m : e->h_ctl->reached_edges;
   e->stats.relaxed_edges = e->h_ctl->relaxed_edges;
   e->stats.relaxed_sources = e->h_ctl->relaxed_sources;
+  e->stats.inner_iterations = (uint64_t)e->h_ctl->iters_total + e->hub_iters;
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, e->ev_t0, e->ev_t1));
   e->stats.ms_device = ms;

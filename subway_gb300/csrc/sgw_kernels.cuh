@@ -46,7 +46,7 @@ struct Ctl {
   uint32_t hub_value;        // single-vertex partition: its value
   uint32_t sel_lo, sel_hi;   // deferral: value range of the pushable active vertices
   uint32_t sel_bin;          //   and the last value bin selected this iteration
-  uint32_t pad0;
+  uint32_t iters_total;      // inner iterations that did work, whole run
   unsigned long long reached_edges;
   unsigned long long relaxed_edges;
   unsigned long long relaxed_sources;
@@ -320,6 +320,163 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
       if (PR) a.qpush[pos] = push[PR ? r : 0];
     }
     run += ((unsigned long long)__popc(keepmask[r]) << 32) | tot;
+  }
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(&a.ctl->tile_done, 1u) == a.num_tiles - 1) {
+      a.ctl->tile_ticket = 0;
+      a.ctl->tile_done = 0;
+    }
+  }
+}
+
+// Integer-family generate with 16 consecutive vertices per lane: the lane
+// reads their labels as two 16-byte words and, only if one of them is
+// active, their 17 node pointers (and values, for the learned policy's
+// selection) as 16-byte words; per-lane counts and edge sums are scanned
+// within the warp, then across the CTA and the tiles exactly as in
+// k_generate, and each lane writes its queued vertices in order.  Same
+// results as k_generate<false>; the label, pointer and value arrays must be
+// 16-byte aligned (the engine's arena is).
+constexpr uint32_t kGenVPerLane = 16;
+__global__ void __launch_bounds__(kGenThreads) k_generate_v(GenArgs a) {
+  __shared__ uint32_t s_tile;
+  __shared__ unsigned long long s_warp[kGenThreads / 32];
+  __shared__ unsigned long long s_prefix;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(&a.ctl->tile_ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  if (tile >= a.num_tiles) {  // stale ticket counter: refuse to index past the tiles
+    if (tid == 0) atomicExch(&a.ctl->error, 4u);
+    return;
+  }
+  const uint32_t v0 = tile * kGenTile + warp * (32 * kGenRounds) + lane * kGenVPerLane;
+  uint32_t sel_lo = 0, sel_hi = 0, sel_bin = 0;
+  if (a.sel_mode & 2) {
+    sel_lo = a.ctl->sel_lo;
+    sel_hi = a.ctl->sel_hi;
+    sel_bin = a.ctl->sel_bin;
+  }
+  const bool full = v0 + kGenVPerLane <= a.n;
+  // activeness bytes of the lane's 16 vertices
+  uint32_t lw[4] = {0, 0, 0, 0}, l1w[4] = {0, 0, 0, 0}, l2w[4] = {0, 0, 0, 0};
+  if (full) {
+    const uint4 x = *reinterpret_cast<const uint4 *>(a.l1 + v0);
+    const uint4 y = *reinterpret_cast<const uint4 *>(a.l2 + v0);
+    l1w[0] = x.x; l1w[1] = x.y; l1w[2] = x.z; l1w[3] = x.w;
+    l2w[0] = y.x; l2w[1] = y.y; l2w[2] = y.z; l2w[3] = y.w;
+  } else {
+    for (uint32_t k = 0; k < kGenVPerLane; ++k)
+      if (v0 + k < a.n) {
+        l1w[k / 4] |= (uint32_t)a.l1[v0 + k] << (8 * (k % 4));
+        l2w[k / 4] |= (uint32_t)a.l2[v0 + k] << (8 * (k % 4));
+      }
+  }
+  uint32_t actmask = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    lw[q] = l1w[q] | l2w[q];
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+      if ((lw[q] >> (8 * b)) & 0xffu) actmask |= 1u << (4 * q + b);
+  }
+  uint32_t keepmask = 0, clearmask = 0, cnt = 0, edges = 0;
+  uint32_t o[kGenVPerLane + 1];  // node pointers; a queued vertex's degree is o[k + 1] - o[k]
+  if (actmask) {
+    uint32_t val[kGenVPerLane];
+    if (full) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint4 p = __ldg(reinterpret_cast<const uint4 *>(a.off + v0) + q);
+        o[4 * q] = p.x; o[4 * q + 1] = p.y; o[4 * q + 2] = p.z; o[4 * q + 3] = p.w;
+      }
+      o[kGenVPerLane] = __ldg(&a.off[v0 + kGenVPerLane]);
+      if (a.sel_mode) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint4 p = reinterpret_cast<const uint4 *>(a.value + v0)[q];
+          val[4 * q] = p.x; val[4 * q + 1] = p.y; val[4 * q + 2] = p.z; val[4 * q + 3] = p.w;
+        }
+      }
+    } else {
+#pragma unroll
+      for (uint32_t k = 0; k <= kGenVPerLane; ++k) o[k] = (v0 + k <= a.n) ? __ldg(&a.off[v0 + k]) : 0u;
+#pragma unroll
+      for (uint32_t k = 0; k < kGenVPerLane; ++k) val[k] = (a.sel_mode && v0 + k < a.n) ? a.value[v0 + k] : 0u;
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kGenVPerLane; ++k) {
+      if (!((actmask >> k) & 1u)) continue;
+      uint32_t d = o[k + 1] - o[k];
+      bool drop = d == 0, defer = false;
+      if (a.sel_mode && !drop) {
+        if (!pushable(a.algo, val[k])) drop = (a.sel_mode & 1) != 0;
+        else if ((a.sel_mode & 2) && !selected(a.algo, val[k], sel_lo, sel_hi, sel_bin)) defer = true;
+      }
+      if (!defer && (a.consume || drop)) clearmask |= 1u << k;
+      if (!drop && !defer) {
+        keepmask |= 1u << k;
+        ++cnt;
+        edges += d;
+      }
+    }
+    if (clearmask) {
+      uint32_t cw[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        cw[q] = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+          if ((clearmask >> (4 * q + b)) & 1u) cw[q] |= 0xffu << (8 * b);
+      }
+      if (full) {
+        *reinterpret_cast<uint4 *>(a.l1 + v0) = make_uint4(l1w[0] & ~cw[0], l1w[1] & ~cw[1], l1w[2] & ~cw[2], l1w[3] & ~cw[3]);
+        *reinterpret_cast<uint4 *>(a.l2 + v0) = make_uint4(l2w[0] & ~cw[0], l2w[1] & ~cw[1], l2w[2] & ~cw[2], l2w[3] & ~cw[3]);
+      } else {
+        for (uint32_t k = 0; k < kGenVPerLane; ++k)
+          if ((clearmask >> k) & 1u) { a.l1[v0 + k] = 0; a.l2[v0 + k] = 0; }
+      }
+    }
+  }
+  const uint32_t seen = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(actmask));
+  const uint32_t incl_c = warp_incl_scan(cnt, lane);
+  const uint32_t incl_e = warp_incl_scan(edges, lane);
+  if (lane == 31) s_warp[warp] = ((unsigned long long)incl_c << 32) | incl_e;
+  if (lane == 0 && seen) atomicAdd(&a.ctl->num_seen, seen);
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long acc = 0;
+#pragma unroll
+    for (int w = 0; w < kGenThreads / 32; ++w) {
+      unsigned long long x = s_warp[w];
+      s_warp[w] = acc;
+      acc += x;
+    }
+    const unsigned long long excl = lookback(tile, acc, a.tflag, a.tagg, a.tincl, a.epoch, a.ctl);
+    s_prefix = excl;
+    if (tile == a.num_tiles - 1) {
+      const unsigned long long tot = excl + acc;
+      const uint32_t c = (uint32_t)(tot >> 32);
+      a.ctl->num_active = c;
+      a.ctl->num_active_edges = tot & 0xffffffffull;
+      a.ptr[c] = (uint32_t)(tot & 0xffffffffull);  // sentinel (subgraph_generator.cu:160)
+    }
+  }
+  __syncthreads();
+  if (keepmask) {
+    const unsigned long long run = s_prefix + s_warp[warp] +
+                                   (((unsigned long long)(incl_c - cnt) << 32) | (incl_e - edges));
+    uint32_t pos = (uint32_t)(run >> 32), ep = (uint32_t)(run & 0xffffffffull);
+#pragma unroll
+    for (uint32_t k = 0; k < kGenVPerLane; ++k) {
+      if ((keepmask >> k) & 1u) {
+        a.queue[pos] = v0 + k;
+        a.ptr[pos] = ep;
+        ++pos;
+        ep += o[k + 1] - o[k];
+      }
+    }
   }
   if (tid == 0) {
     __threadfence();
@@ -880,7 +1037,10 @@ __device__ __forceinline__ void relax_tile_phase(const RelaxArgs &a, TileSmem &s
     if (blockIdx.x == 0) {
       a.ctl->upd[(a.iter + 1) & 3u] = 0;
       a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
-      if (!skip) atomicAdd(&a.ctl->iters_run, 1u);
+      if (!skip) {
+        atomicAdd(&a.ctl->iters_run, 1u);
+        atomicAdd(&a.ctl->iters_total, 1u);
+      }
     }
   }
   __syncthreads();
@@ -1032,7 +1192,10 @@ __global__ void __launch_bounds__(kRelaxThreads, 4) k_relax_warp(RelaxArgs a) {
     if (blockIdx.x == 0) {
       a.ctl->upd[(a.iter + 1) & 3u] = 0;
       a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
-      if (!skip) atomicAdd(&a.ctl->iters_run, 1u);
+      if (!skip) {
+        atomicAdd(&a.ctl->iters_run, 1u);
+        atomicAdd(&a.ctl->iters_total, 1u);
+      }
     }
   }
   __syncthreads();
@@ -1323,7 +1486,10 @@ __global__ void __launch_bounds__(kRelaxThreads) k_pr_tile(PrArgs a) {
     if (blockIdx.x == 0) {
       a.ctl->upd[(a.iter + 1) & 3u] = 0;
       a.ctl->wl_count[(a.iter + 1) & 3u] = 0;
-      if (!skip) atomicAdd(&a.ctl->iters_run, 1u);
+      if (!skip) {
+        atomicAdd(&a.ctl->iters_run, 1u);
+        atomicAdd(&a.ctl->iters_total, 1u);
+      }
     }
   }
   __syncthreads();
