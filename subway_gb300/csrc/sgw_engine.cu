@@ -677,10 +677,12 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
 // Relaxation of one resident partition: sync = one pass; async = mixLabels
 // then inner iterations until no relaxation improves (or max_inner).
 // Inner iterations are counted on the device (Ctl::iters_total, refreshed
-// into the statistics by every control-block read); with sync_always false a
-// partition whose inner cap is reached returns without waiting for it, so
-// the host goes on enqueueing the next partition's work (*iters_out is then
-// 0: unknown until the next read).
+// into the statistics by every control-block read).  With sync_always false
+// a partition whose inner cap is reached returns without waiting for it
+// (*iters_out is then 0: unknown until the next read).  The learned policy
+// keeps the wait: letting the host run ahead put more gathers beside each
+// relaxation and made both slower (RMAT-24 SSSP-async: 12.2 against 17.0
+// GTEPS).
 int process_resident(sgw_engine *e, const Part &q, uint32_t b, uint32_t *iters_out, bool sync_always = true) {
   const bool async = e->params.mode == SGW_ASYNC;
   // upd, wl_count, iters_run
@@ -1003,7 +1005,7 @@ int process_iteration_ranges(sgw_engine *e) {
       for (uint32_t s = j.s; s < j.s_end; ++s) pred = std::max(pred, e->h_rstat[s].pred);
       const bool cappable = kept || (e->opts.sched_flags & SGW_SCHED_CAP_COMPACT);
       e->range_inner_cap = cappable && (double)pred >= thr ? (e->opts.sched_inner ? e->opts.sched_inner : 2u) : 0u;
-      const int st = process_resident(e, q, (uint32_t)j.buf, &inner, e->trace_on);
+      const int st = process_resident(e, q, (uint32_t)j.buf, &inner);
       e->cur_streamed = 0;
       e->range_inner_cap = 0;
       TRY(st);

@@ -125,30 +125,54 @@ __device__ __forceinline__ uint32_t wait_tile_flag(const uint32_t *flag, uint32_
   return 0;
 }
 
-// Decoupled look-back for tile `tile` with aggregate `agg`, run by one thread.
-// Values are packed (count << 32) | edges; both sums stay below 2^32 so the
-// packed add never carries.  Returns the exclusive prefix of the tile.
-__device__ __forceinline__ unsigned long long lookback(
-    uint32_t tile, unsigned long long agg, uint32_t *tflag,
-    unsigned long long *tagg, unsigned long long *tincl, uint32_t epoch, Ctl *ctl) {
+// Decoupled look-back for tile `tile` with aggregate `agg`, run by a whole
+// warp.  Values are packed (count << 32) | edges; both sums stay below 2^32
+// so the packed add never carries.  Lane k examines predecessor
+// tile - 1 - k - 32 r, so one round trip covers 32 predecessors; the sum
+// stops at the nearest one whose inclusive prefix is published.  (At 2^28
+// vertices, 65536 tiles, a single-thread walk made the scan's critical path
+// milliseconds long.)  Called by all lanes of one warp; returns the exclusive
+// prefix on every lane.
+__device__ __forceinline__ unsigned long long lookback_warp(
+    uint32_t tile, unsigned long long agg, uint32_t *tflag, unsigned long long *tagg,
+    unsigned long long *tincl, uint32_t epoch, Ctl *ctl, int lane) {
   if (tile == 0) {
-    st_relaxed_u64(&tincl[0], agg);
-    st_release_u32(&tflag[0], (epoch << 2) | 2u);
+    if (lane == 0) {
+      st_relaxed_u64(&tincl[0], agg);
+      st_release_u32(&tflag[0], (epoch << 2) | 2u);
+    }
     return 0ull;
   }
-  st_relaxed_u64(&tagg[tile], agg);
-  st_release_u32(&tflag[tile], (epoch << 2) | 1u);
-  unsigned long long excl = 0;
-  int32_t j = (int32_t)tile - 1;
-  while (j >= 0) {
-    uint32_t f = wait_tile_flag(&tflag[j], epoch, ctl);
-    if (f == 0) break;  // timed out: error recorded, prefix is garbage
-    if ((f & 3u) == 2u) { excl += ld_relaxed_u64(&tincl[j]); break; }
-    excl += ld_relaxed_u64(&tagg[j]);
-    --j;
+  if (lane == 0) {
+    st_relaxed_u64(&tagg[tile], agg);
+    st_release_u32(&tflag[tile], (epoch << 2) | 1u);
   }
-  st_relaxed_u64(&tincl[tile], excl + agg);
-  st_release_u32(&tflag[tile], (epoch << 2) | 2u);
+  unsigned long long excl = 0;
+  for (int32_t base = (int32_t)tile - 1;; base -= 32) {
+    const int32_t j = base - lane;
+    uint32_t status = 2u;  // before tile 0: an inclusive prefix of 0
+    unsigned long long v = 0;
+    if (j >= 0) {
+      const uint32_t f = wait_tile_flag(&tflag[j], epoch, ctl);
+      if (f == 0) {
+        status = 3u;  // timed out: error recorded, prefix is garbage
+      } else {
+        status = f & 3u;
+        v = status == 2u ? ld_relaxed_u64(&tincl[j]) : ld_relaxed_u64(&tagg[j]);
+      }
+    }
+    const uint32_t stop = __ballot_sync(0xffffffffu, status >= 2u);
+    const int first = stop ? __ffs(stop) - 1 : 31;
+    if (lane > first) v = 0;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    excl += v;
+    if (stop) break;
+  }
+  if (lane == 0) {
+    st_relaxed_u64(&tincl[tile], excl + agg);
+    st_release_u32(&tflag[tile], (epoch << 2) | 2u);
+  }
   return excl;
 }
 
@@ -287,23 +311,27 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
     if (seen) atomicAdd(&a.ctl->num_seen, seen);
   }
   __syncthreads();
-  if (tid == 0) {
+  if (warp == 0) {
     unsigned long long acc = 0;
+    if (lane == 0) {
 #pragma unroll
-    for (int w = 0; w < kGenThreads / 32; ++w) {
-      unsigned long long x = s_warp[w];
-      s_warp[w] = acc;
-      acc += x;
+      for (int w = 0; w < kGenThreads / 32; ++w) {
+        unsigned long long x = s_warp[w];
+        s_warp[w] = acc;
+        acc += x;
+      }
     }
-    const unsigned long long excl =
-        lookback(tile, acc, a.tflag, a.tagg, a.tincl, a.epoch, a.ctl);
-    s_prefix = excl;
-    if (tile == a.num_tiles - 1) {
-      const unsigned long long tot = excl + acc;
-      const uint32_t cnt = (uint32_t)(tot >> 32);
-      a.ctl->num_active = cnt;
-      a.ctl->num_active_edges = tot & 0xffffffffull;
-      a.ptr[cnt] = (uint32_t)(tot & 0xffffffffull);  // sentinel (subgraph_generator.cu:160)
+    acc = __shfl_sync(0xffffffffu, acc, 0);
+    const unsigned long long excl = lookback_warp(tile, acc, a.tflag, a.tagg, a.tincl, a.epoch, a.ctl, lane);
+    if (lane == 0) {
+      s_prefix = excl;
+      if (tile == a.num_tiles - 1) {
+        const unsigned long long tot = excl + acc;
+        const uint32_t cnt = (uint32_t)(tot >> 32);
+        a.ctl->num_active = cnt;
+        a.ctl->num_active_edges = tot & 0xffffffffull;
+        a.ptr[cnt] = (uint32_t)(tot & 0xffffffffull);  // sentinel (subgraph_generator.cu:160)
+      }
     }
   }
   __syncthreads();
@@ -445,22 +473,27 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_v(GenArgs a) {
   if (lane == 31) s_warp[warp] = ((unsigned long long)incl_c << 32) | incl_e;
   if (lane == 0 && seen) atomicAdd(&a.ctl->num_seen, seen);
   __syncthreads();
-  if (tid == 0) {
+  if (warp == 0) {
     unsigned long long acc = 0;
+    if (lane == 0) {
 #pragma unroll
-    for (int w = 0; w < kGenThreads / 32; ++w) {
-      unsigned long long x = s_warp[w];
-      s_warp[w] = acc;
-      acc += x;
+      for (int w = 0; w < kGenThreads / 32; ++w) {
+        unsigned long long x = s_warp[w];
+        s_warp[w] = acc;
+        acc += x;
+      }
     }
-    const unsigned long long excl = lookback(tile, acc, a.tflag, a.tagg, a.tincl, a.epoch, a.ctl);
-    s_prefix = excl;
-    if (tile == a.num_tiles - 1) {
-      const unsigned long long tot = excl + acc;
-      const uint32_t c = (uint32_t)(tot >> 32);
-      a.ctl->num_active = c;
-      a.ctl->num_active_edges = tot & 0xffffffffull;
-      a.ptr[c] = (uint32_t)(tot & 0xffffffffull);  // sentinel (subgraph_generator.cu:160)
+    acc = __shfl_sync(0xffffffffu, acc, 0);
+    const unsigned long long excl = lookback_warp(tile, acc, a.tflag, a.tagg, a.tincl, a.epoch, a.ctl, lane);
+    if (lane == 0) {
+      s_prefix = excl;
+      if (tile == a.num_tiles - 1) {
+        const unsigned long long tot = excl + acc;
+        const uint32_t c = (uint32_t)(tot >> 32);
+        a.ctl->num_active = c;
+        a.ctl->num_active_edges = tot & 0xffffffffull;
+        a.ptr[c] = (uint32_t)(tot & 0xffffffffull);  // sentinel (subgraph_generator.cu:160)
+      }
     }
   }
   __syncthreads();
