@@ -291,3 +291,33 @@ def test_wide_weights_fall_back_to_full_records(gpu, orc):
             vals, st = eng.run(algo, mode, 0)
             assert np.array_equal(vals, _oracle(orc, g, algo, 0)), (algo, mode)
     assert st["h2d_bytes"] % 8 == 0
+
+
+@pytest.mark.parametrize("n", [1, 5, 17, 4097, 8191])
+def test_odd_vertex_counts(gpu, orc, n):
+    """Vertex counts that are not multiples of 16 or of the 4096-vertex scan
+    tile (partial lane groups and tiles in the generate step), a single
+    vertex, and a vertex count below one lane's 16: every algorithm, both
+    modes, plain and learned schedules, bit-exact."""
+    rng = np.random.default_rng(n)
+    m0 = 6 * n
+    src = rng.integers(0, n, m0)
+    dst = rng.integers(0, n, m0)
+    keep = src != dst
+    pairs = np.unique(np.stack([src[keep], dst[keep]], 1), axis=0) if keep.any() else np.zeros((0, 2), np.int64)
+    npt = np.zeros(n + 1, np.uint32)
+    np.add.at(npt, pairs[:, 0] + 1, 1)
+    npt = np.cumsum(npt).astype(np.uint32)
+    w = (1 + (pairs[:, 0] * 5 + pairs[:, 1] * 3) % 60).astype(np.uint32)
+    edges = np.stack([pairs[:, 1].astype(np.uint32), w], 1)
+    g = gpu.Graph.from_csr(npt, edges, True)
+    budget = 18 * n + 96 * 1024 + max(64, g.m // 3) * 8 * 3
+    s0 = int(np.argmax(np.diff(npt))) if g.m else 0
+    for policy in ("plain", "learned"):
+        eng = gpu.Engine(g, budget_bytes=budget, num_buffers=3 if policy == "learned" else 0)
+        if policy == "learned":
+            eng.set_policy("learned")
+        for algo in ALGS:
+            for mode in MODES:
+                vals, _ = eng.run(algo, mode, s0)
+                assert np.array_equal(vals, _oracle(orc, g, algo, s0)), (n, policy, algo, mode)
