@@ -127,12 +127,13 @@ __device__ __forceinline__ uint32_t wait_tile_flag(const uint32_t *flag, uint32_
 
 // Decoupled look-back for tile `tile` with aggregate `agg`, run by a whole
 // warp.  Values are packed (count << 32) | edges; both sums stay below 2^32
-// so the packed add never carries.  Lane k examines predecessor
-// tile - 1 - k - 32 r, so one round trip covers 32 predecessors; the sum
-// stops at the nearest one whose inclusive prefix is published.  (At 2^28
-// vertices, 65536 tiles, a single-thread walk made the scan's critical path
-// milliseconds long.)  Called by all lanes of one warp; returns the exclusive
-// prefix on every lane.
+// so the packed add never carries.  Lane k examines predecessors
+// tile - 1 - (4 k + q) - 128 r, q < 4, so one round covers 128 predecessors
+// (hundreds of tiles run at once, and a tile late in that wave finds only
+// aggregates until it reaches the previous wave); the sum stops at the
+// nearest predecessor whose inclusive prefix is published.  Called by all
+// lanes of one warp; returns the exclusive prefix on every lane.
+constexpr int kLookPer = 4;
 __device__ __forceinline__ unsigned long long lookback_warp(
     uint32_t tile, unsigned long long agg, uint32_t *tflag, unsigned long long *tagg,
     unsigned long long *tincl, uint32_t epoch, Ctl *ctl, int lane) {
@@ -148,25 +149,40 @@ __device__ __forceinline__ unsigned long long lookback_warp(
     st_release_u32(&tflag[tile], (epoch << 2) | 1u);
   }
   unsigned long long excl = 0;
-  for (int32_t base = (int32_t)tile - 1;; base -= 32) {
-    const int32_t j = base - lane;
-    uint32_t status = 2u;  // before tile 0: an inclusive prefix of 0
-    unsigned long long v = 0;
-    if (j >= 0) {
+  for (int32_t base = (int32_t)tile - 1;; base -= 32 * kLookPer) {
+    unsigned long long v[kLookPer];
+    int stop_q = kLookPer;  // nearest of this lane's predecessors that ends the walk
+#pragma unroll
+    for (int q = 0; q < kLookPer; ++q) {
+      const int32_t j = base - (lane * kLookPer + q);
+      v[q] = 0;
+      if (j < 0) {  // before tile 0: an inclusive prefix of 0
+        if (stop_q == kLookPer) stop_q = q;
+        continue;
+      }
       const uint32_t f = wait_tile_flag(&tflag[j], epoch, ctl);
-      if (f == 0) {
-        status = 3u;  // timed out: error recorded, prefix is garbage
+      if (f == 0) {  // timed out: error recorded, prefix is garbage
+        if (stop_q == kLookPer) stop_q = q;
+        continue;
+      }
+      if ((f & 3u) == 2u) {
+        v[q] = ld_relaxed_u64(&tincl[j]);
+        if (stop_q == kLookPer) stop_q = q;
       } else {
-        status = f & 3u;
-        v = status == 2u ? ld_relaxed_u64(&tincl[j]) : ld_relaxed_u64(&tagg[j]);
+        v[q] = ld_relaxed_u64(&tagg[j]);
       }
     }
-    const uint32_t stop = __ballot_sync(0xffffffffu, status >= 2u);
-    const int first = stop ? __ffs(stop) - 1 : 31;
-    if (lane > first) v = 0;
+    // the walk ends at the nearest (lowest lane, then lowest q) stopping predecessor
+    const uint32_t stop = __ballot_sync(0xffffffffu, stop_q < kLookPer);
+    const int first = stop ? __ffs(stop) - 1 : 32;
+    const int first_q = __shfl_sync(0xffffffffu, stop_q, first < 32 ? first : 0);
+    unsigned long long s = 0;
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-    excl += v;
+    for (int q = 0; q < kLookPer; ++q)
+      if (lane < first || (lane == first && q <= first_q)) s += v[q];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+    excl += s;
     if (stop) break;
   }
   if (lane == 0) {
