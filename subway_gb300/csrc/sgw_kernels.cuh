@@ -151,21 +151,27 @@ __device__ __forceinline__ unsigned long long lookback_warp(
   unsigned long long excl = 0;
   for (int32_t base = (int32_t)tile - 1;; base -= 32 * kLookPer) {
     unsigned long long v[kLookPer];
+    uint32_t f[kLookPer];
     int stop_q = kLookPer;  // nearest of this lane's predecessors that ends the walk
+    // the lane's 4 flags are read together; only a flag not yet published
+    // for this epoch is waited on (bounded)
+#pragma unroll
+    for (int q = 0; q < kLookPer; ++q) {
+      const int32_t j = base - (lane * kLookPer + q);
+      f[q] = j >= 0 ? ld_acquire_u32(&tflag[j]) : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < kLookPer; ++q) {
+      const int32_t j = base - (lane * kLookPer + q);
+      if (j >= 0 && !((f[q] >> 2) == epoch && (f[q] & 3u) != 0)) f[q] = wait_tile_flag(&tflag[j], epoch, ctl);
+    }
 #pragma unroll
     for (int q = 0; q < kLookPer; ++q) {
       const int32_t j = base - (lane * kLookPer + q);
       v[q] = 0;
-      if (j < 0) {  // before tile 0: an inclusive prefix of 0
+      if (j < 0 || f[q] == 0) {  // before tile 0 (an inclusive 0), or timed out (error recorded)
         if (stop_q == kLookPer) stop_q = q;
-        continue;
-      }
-      const uint32_t f = wait_tile_flag(&tflag[j], epoch, ctl);
-      if (f == 0) {  // timed out: error recorded, prefix is garbage
-        if (stop_q == kLookPer) stop_q = q;
-        continue;
-      }
-      if ((f & 3u) == 2u) {
+      } else if ((f[q] & 3u) == 2u) {
         v[q] = ld_relaxed_u64(&tincl[j]);
         if (stop_q == kLookPer) stop_q = q;
       } else {
