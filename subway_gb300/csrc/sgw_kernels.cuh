@@ -128,12 +128,13 @@ __device__ __forceinline__ uint32_t wait_tile_flag(const uint32_t *flag, uint32_
 // Decoupled look-back for tile `tile` with aggregate `agg`, run by a whole
 // warp.  Values are packed (count << 32) | edges; both sums stay below 2^32
 // so the packed add never carries.  Lane k examines predecessors
-// tile - 1 - (4 k + q) - 128 r, q < 4, so one round covers 128 predecessors
-// (hundreds of tiles run at once, and a tile late in that wave finds only
-// aggregates until it reaches the previous wave); the sum stops at the
-// nearest predecessor whose inclusive prefix is published.  Called by all
-// lanes of one warp; returns the exclusive prefix on every lane.
-constexpr int kLookPer = 4;
+// tile - 1 - (kLookPer k + q) - 32 kLookPer r, q < kLookPer, so one round
+// covers 32 kLookPer predecessors; the sum stops at the nearest predecessor
+// whose inclusive prefix is published.  One per lane measured best: with 4
+// per lane (128 per round) a tile waits on more unpublished neighbours and
+// the scan ran 30-40% longer.  Called by all lanes of one warp; returns the
+// exclusive prefix on every lane.
+constexpr int kLookPer = 1;
 __device__ __forceinline__ unsigned long long lookback_warp(
     uint32_t tile, unsigned long long agg, uint32_t *tflag, unsigned long long *tagg,
     unsigned long long *tincl, uint32_t epoch, Ctl *ctl, int lane) {
