@@ -228,6 +228,7 @@ def run_ours(a, dist):
             e.set_policy("learned", model)
             e.model_name = "persistence" if model is None else Path(a.model or scheduler.DEFAULT_MODEL).name
         e.edge_buffers = nb or 2
+        e.dma_gbs = round(e.dma_rate(), 1)
         return e
 
     def measure(eng):
@@ -318,6 +319,7 @@ def run_ours(a, dist):
         "config": workload_config(a, {"policy": "plain" if a.policy == "plain" else "learned",
                                       "scheduler_model": getattr(eng, "model_name", None),
                                       "edge_buffers": getattr(eng, "edge_buffers", 2),
+                                      "transfer_copy_dma_gbs": getattr(eng, "dma_gbs", None),
                                       "transfer_record_bytes": 4 if (weighted and not a.no_pack) or not weighted else 8}),
         "plain_policy": plain_summary,
         "learned_over_plain": (None if not plain_summary else

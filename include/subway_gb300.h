@@ -340,6 +340,10 @@ int sgw_set_policy(sgw_engine *e, int policy, const sgw_mlp *model);
  * transfers and relaxation overlapped), else 2 (larger partitions pay more
  * than residency of a small slice). */
 int sgw_sched_buffers(const sgw_graph *g, uint64_t budget_bytes, uint32_t *num_buffers);
+/* Host-to-device DMA rate (GB/s) from the engine's transfer copy, timed at
+ * engine creation (-1 when the copy is too small to time).  The learned
+ * policy streams whole ranges only when it is at least 120 GB/s. */
+int sgw_engine_dma_rate(const sgw_engine *e, double *gbs);
 
 /* Per range and global iteration of a SGW_POLICY_LEARNED run (recorded while
  * the trace is enabled): the features, the prediction and what was done. */

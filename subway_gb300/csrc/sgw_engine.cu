@@ -87,6 +87,7 @@ struct sgw_engine {
   const void *h_src = nullptr;             // host view of the transfer records
   // Split form: weights below 256 that do not pack beside the vertex id
   // travel as a separate byte stream (5 bytes per edge instead of 8).
+  double dma_gbs = -1.0;                   // measured DMA rate from the transfer copy (-1: not timed)
   bool split = false;
   bool use_w = false;                      // this run reads the weight stream
   const uint4 *d_host_w16 = nullptr;       // device view of the weight stream
@@ -176,6 +177,38 @@ int check_ctl_error(sgw_engine *e) {
   if (err == 3) return fail(SGW_ERANGE, "chunk list overflow");
   if (err == 4) return fail(SGW_ESTATE, "scan ticket counter out of step");
   return fail(SGW_ECUDA, "device error code %u", err);
+}
+
+// Whole-range streaming moves records by DMA from the transfer copy.  On
+// some boxes of one pool that DMA ran at a fraction of the host-link rate
+// while the gather kernels' reads did not (the learned policy then lost to
+// the plain one), so the engine times a few copies at creation; the learned
+// policy streams whole ranges only when the rate is at least kMinStreamGBs.
+// Copies below 64 MB are too short to time: the rate is then taken as good.
+constexpr double kMinStreamGBs = 120.0;
+int probe_stream_dma(sgw_engine *e) {
+  e->dma_gbs = -1.0;
+  const size_t bytes = std::min<size_t>(std::min<size_t>(e->packed_bytes, (size_t)e->cap * 4 * e->W),
+                                        size_t(256) << 20) & ~size_t(15);
+  if (!e->h_packed || bytes < (size_t(64) << 20)) return SGW_OK;
+  cudaEvent_t a = nullptr, b = nullptr;
+  CK(cudaEventCreate(&a));
+  if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return fail(SGW_ECUDA, "event creation"); }
+  double best = 0.0;
+  int st = SGW_OK;
+  for (int i = 0; i < 4 && st == SGW_OK; ++i) {  // the first copy warms up
+    cudaEventRecord(a, e->s_copy);
+    cudaMemcpyAsync(e->d_buf[0], e->h_packed, bytes, cudaMemcpyHostToDevice, e->s_copy);
+    cudaEventRecord(b, e->s_copy);
+    if (cudaEventSynchronize(b) != cudaSuccess) { st = fail(SGW_ECUDA, "transfer-copy DMA probe"); break; }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (i > 0 && ms > 0) best = std::max(best, (double)bytes / (ms * 1e6));
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (st == SGW_OK) e->dma_gbs = best;
+  return st;
 }
 
 int read_ctl(sgw_engine *e) {
@@ -917,7 +950,8 @@ int process_iteration_ranges(sgw_engine *e) {
       act[s] = SGW_ACT_COMPACT;
     }
   }
-  const size_t keep_slots = e->nbuf > 2 ? e->nbuf - 2 : 0;
+  const bool dma_ok = e->dma_gbs < 0.0 || e->dma_gbs >= kMinStreamGBs;
+  const size_t keep_slots = (e->nbuf > 2 && dma_ok) ? e->nbuf - 2 : 0;
   if (stream_cand.size() > keep_slots) {
     std::sort(stream_cand.begin(), stream_cand.end(),
               [](const std::pair<double, uint32_t> &x, const std::pair<double, uint32_t> &y) {
@@ -1278,7 +1312,8 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_tflag, 0, 4ull * e->num_tiles, e->s_comp);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->s_comp);
   if (ce != cudaSuccess) return cleanup(fail(SGW_ECUDA, "engine setup copies: %s", cudaGetErrorString(ce)));
-  (void)st;
+  st = probe_stream_dma(e);
+  if (st != SGW_OK) return cleanup(st);
   *out = e;
   return SGW_OK;
 }
@@ -1385,6 +1420,12 @@ int sgw_process_partition(sgw_engine *e, uint32_t i, uint32_t *inner_iterations)
   if (i == 0) e->gitr += 1;
   trace_partition(e, i, iters);
   if (inner_iterations) *inner_iterations = iters;
+  return SGW_OK;
+}
+
+int sgw_engine_dma_rate(const sgw_engine *e, double *gbs) {
+  if (!e || !gbs) return fail(SGW_EINVAL, "null argument");
+  *gbs = e->dma_gbs;
   return SGW_OK;
 }
 

@@ -108,6 +108,7 @@ _PROTOS = {
     "sgw_mlp_load": (C.c_int, [C.c_int, C.c_char_p, C.POINTER(_P)]),
     "sgw_set_policy": (C.c_int, [_P, C.c_int, _P]),
     "sgw_sched_buffers": (C.c_int, [_P, C.c_uint64, _u32p]),
+    "sgw_engine_dma_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "sgw_batch_create": (C.c_int, [_P, C.POINTER(EngineOpts), C.c_uint32, C.POINTER(_P)]),
     "sgw_batch_destroy": (C.c_int, [_P]),
     "sgw_batch_device_bytes": (C.c_int, [_P, _u64p]),
@@ -333,6 +334,12 @@ class Engine:
         v = C.c_uint64()
         check(lib().sgw_engine_device_bytes(self.h, C.byref(v)), "device_bytes")
         return v.value
+
+    def dma_rate(self) -> float:
+        """DMA rate (GB/s) from the transfer copy timed at creation, -1 if not timed."""
+        g = C.c_double(0)
+        check(lib().sgw_engine_dma_rate(self.h, C.byref(g)), "sgw_engine_dma_rate")
+        return g.value
 
     def run(self, algo, mode, source=0, out=None, **kw):
         p = run_params(algo, mode, source, **kw)
