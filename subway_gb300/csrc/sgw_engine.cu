@@ -33,7 +33,7 @@ using namespace sgw;
 
 namespace {
 
-enum KClass { K_GENERATE = 0, K_PLAN, K_GATHER, K_RELAX, K_NCLASS };
+enum KClass { K_GENERATE = 0, K_PLAN, K_GATHER, K_RELAX, K_STREAM, K_NCLASS };
 
 struct ProfEvent {
   int cls;
@@ -88,6 +88,8 @@ struct sgw_engine {
   // Split form: weights below 256 that do not pack beside the vertex id
   // travel as a separate byte stream (5 bytes per edge instead of 8).
   double dma_gbs = -1.0;                   // measured DMA rate from the transfer copy (-1: not timed)
+  uint64_t stream_bytes = 0;               // whole-range copies timed so far (profiling)
+  double stream_ms = 0.0;
   bool split = false;
   bool use_w = false;                      // this run reads the weight stream
   const uint4 *d_host_w16 = nullptr;       // device view of the weight stream
@@ -154,8 +156,11 @@ int prof_end(sgw_engine *e, cudaStream_t s, size_t slot) {
   return SGW_OK;
 }
 
+// Whole-range DMA rate below which the learned policy stops streaming.
+constexpr double kMinStreamGBs = 120.0;
+
 int prof_collect(sgw_engine *e) {
-  double ms[K_NCLASS] = {0, 0, 0, 0};
+  double ms[K_NCLASS] = {0, 0, 0, 0, 0};
   for (size_t i = 0; i < e->prof_used; ++i) {
     float t = 0;
     CK(cudaEventElapsedTime(&t, e->prof[i].a, e->prof[i].b));
@@ -164,8 +169,15 @@ int prof_collect(sgw_engine *e) {
   e->prof_used = 0;
   e->stats.ms_generate += ms[K_GENERATE];
   e->stats.ms_partition += ms[K_PLAN];
-  e->stats.ms_gather += ms[K_GATHER];
+  e->stats.ms_gather += ms[K_GATHER] + ms[K_STREAM];  // transfers of both kinds
   e->stats.ms_relax += ms[K_RELAX];
+  // the whole-range copies' own rate: if it falls below what the policy
+  // assumes, later runs send compacted edges only
+  e->stream_ms += ms[K_STREAM];
+  if (e->stream_bytes >= (uint64_t(256) << 20) && e->stream_ms > 0) {
+    const double rate = (double)e->stream_bytes / (e->stream_ms * 1e6);
+    if (rate < kMinStreamGBs) e->dma_gbs = rate;
+  }
   return SGW_OK;
 }
 
@@ -180,12 +192,12 @@ int check_ctl_error(sgw_engine *e) {
 }
 
 // Whole-range streaming moves records by DMA from the transfer copy.  On
-// some boxes of one pool that DMA ran at a fraction of the host-link rate
-// while the gather kernels' reads did not (the learned policy then lost to
-// the plain one), so the engine times a few copies at creation; the learned
-// policy streams whole ranges only when the rate is at least kMinStreamGBs.
-// Copies below 64 MB are too short to time: the rate is then taken as good.
-constexpr double kMinStreamGBs = 120.0;
+// some boxes of one pool the learned policy's transfers ran at half their
+// usual rate while the plain policy's gathers did not, so the engine times a
+// few DMA copies at creation (and, when profiling, the streamed copies of
+// every run, in prof_collect); the learned policy streams whole ranges only
+// while the rate is at least kMinStreamGBs.  Copies below 64 MB are too short
+// to time: the rate is then taken as good.
 int probe_stream_dma(sgw_engine *e) {
   e->dma_gbs = -1.0;
   const size_t bytes = std::min<size_t>(std::min<size_t>(e->packed_bytes, (size_t)e->cap * 4 * e->W),
@@ -886,7 +898,8 @@ int range_transfer(sgw_engine *e, Job &j, int b) {
     const size_t bytes = (size_t)(r.e1 - r.e0) * esz;
     CK(cudaStreamWaitEvent(e->s_copy, e->ev_free[b], 0));
     size_t slot = 0;
-    TRY(prof_begin(e, K_GATHER, e->s_copy, &slot));
+    TRY(prof_begin(e, K_STREAM, e->s_copy, &slot));
+    e->stream_bytes += bytes + (e->use_w ? (size_t)(r.e1 - r.e0) : 0);
     // a whole range is contiguous: one DMA copy, no SM time taken from the
     // relaxation running on the compute stream
     CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->h_src + (size_t)r.e0 * esz, bytes,
