@@ -1220,18 +1220,15 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
 }
 
 // Warp-tile form of k_relax_tile: each warp takes 32 partition sources at a
-// time and expands their edges on its own (warp scan of the degrees, owner
-// found by binary search in the warp's slice of shared memory), so warps
-// never wait on each other: a warp that runs out of tiles adds its counters
+// time and expands their edges on its own (warp scan of the degrees, each
+// edge's owner found with warp votes and shuffles, no shared memory), so
+// warps never wait on each other: a warp that runs out of tiles adds its counters
 // to the CTA's in shared memory and leaves, and the last warp of the CTA to
 // leave publishes them.  Sources above tile_degree_max go to the chunk list
 // as in the CTA form.
 constexpr int kWarpsPerCta = kRelaxThreads / 32;
 template <int ALGO, bool ASYNC, int W>
 __global__ void __launch_bounds__(kRelaxThreads, 4) k_relax_warp(RelaxArgs a) {
-  __shared__ uint32_t s_excl[kWarpsPerCta][33];
-  __shared__ uint32_t s_boff[kWarpsPerCta][32];
-  __shared__ uint32_t s_val[kWarpsPerCta][32];
   __shared__ int s_skip;
   __shared__ unsigned long long s_edges, s_srcs;
   __shared__ uint32_t s_any, s_done;
@@ -1256,9 +1253,6 @@ __global__ void __launch_bounds__(kRelaxThreads, 4) k_relax_warp(RelaxArgs a) {
   }
   __syncthreads();
   if (s_skip) return;
-  uint32_t *const excl_s = s_excl[wid];
-  uint32_t *const boff_s = s_boff[wid];
-  uint32_t *const val_s = s_val[wid];
   bool any_update = false;
   unsigned long long my_edges = 0, my_srcs = 0;
   const uint32_t ntiles = (a.size + 31u) / 32u;
@@ -1313,30 +1307,33 @@ __global__ void __launch_bounds__(kRelaxThreads, 4) k_relax_warp(RelaxArgs a) {
     if (d > a.tile_degree_max) d = 0;
     const uint32_t incl = warp_incl_scan(d, lane);
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    __syncwarp();
-    excl_s[lane] = incl - d;
-    boff_s[lane] = boff;
-    val_s[lane] = val;
-    __syncwarp();
+    const uint32_t excl = incl - d;
+    const uint32_t owners = __ballot_sync(0xffffffffu, d > 0);  // lanes owning edges, in edge order
     my_edges += total;
-    for (uint32_t j0 = lane; j0 < total; j0 += 32u * kRelaxUnroll) {
+    for (uint32_t w0 = 0; w0 < total; w0 += 32u * kRelaxUnroll) {
       uint32_t dst[kRelaxUnroll], w[kRelaxUnroll], sv[kRelaxUnroll], cur[kRelaxUnroll];
       bool ok[kRelaxUnroll];
 #pragma unroll
       for (int q = 0; q < kRelaxUnroll; ++q) {
-        const uint32_t j = j0 + 32u * q;
+        // window of 32 edges [wb, wb + 32), lane i takes edge wb + i; its
+        // owner is found with votes instead of a search: the owners whose
+        // range starts at or before wb, plus those starting inside the
+        // window up to edge wb + i, count the owner's rank among `owners`
+        const uint32_t wb = w0 + 32u * q;
+        const uint32_t j = wb + lane;
         ok[q] = j < total;
+        const bool own = d > 0;
+        const uint32_t starts =
+            __reduce_or_sync(0xffffffffu, (own && excl > wb && excl < wb + 32u) ? (1u << (excl - wb)) : 0u);
+        const uint32_t before = __popc(__ballot_sync(0xffffffffu, own && excl <= wb));
+        const uint32_t rank = before + __popc(starts & ((2u << lane) - 1u)) - 1u;
+        const int k = __fns(owners, 0, (int)rank + 1);
+        const uint32_t kb = __shfl_sync(0xffffffffu, boff, k & 31);
+        const uint32_t ke = __shfl_sync(0xffffffffu, excl, k & 31);
+        const uint32_t kv = __shfl_sync(0xffffffffu, val, k & 31);
         if (ok[q]) {
-          // last lane k with excl[k] <= j (lanes with d == 0 share offsets;
-          // the last one with that offset owns edge j)
-          uint32_t lo = 0, hi = 32;
-          while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (excl_s[mid] <= j) lo = mid + 1; else hi = mid;
-          }
-          const uint32_t k = lo - 1;
-          load_edge<W>(a.buf, boff_s[k] + (j - excl_s[k]), a.pbits, dst[q], w[q], a.wbuf);
-          sv[q] = val_s[k];
+          load_edge<W>(a.buf, kb + (j - ke), a.pbits, dst[q], w[q], a.wbuf);
+          sv[q] = kv;
         }
       }
 #pragma unroll
