@@ -445,7 +445,9 @@ int launch_generate(sgw_engine *e, int consume) {
     a.sel_mode = (e->opts.sched_flags & SGW_SCHED_KEEP_IDLE) ? 0 : 1;
     a.algo = e->params.algo;
     a.value = e->d_value;
-    if (defer_permille(e)) {
+    // sync BFS queues one level at a time: nothing to order, so no passes
+    const bool level_sync = e->params.algo == SGW_BFS && e->params.mode == SGW_SYNC;
+    if (defer_permille(e) && !level_sync) {
       a.sel_mode |= 2;
       TRY(launch_select(e));
     }
