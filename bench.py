@@ -7,7 +7,11 @@ seeded sources from the largest weakly connected component, device-memory
 budget 1 GB (about 0.46 of the 2.1 GB of edge records stays resident).
 
 Metric: GTEPS = reached edges (Graph500 m_reached) / processing time, plus
-the bytes the device read from host memory per run.
+the bytes the device read from host memory per run.  Both schedules are
+timed, the plain one (the reference's: every active edge compacted and sent
+each iteration, async partitions relaxed to convergence) first; the learned
+one is the headline line and `plain_policy` / `learned_over_plain` carry the
+comparison (speed-up, H2D bytes ratio, mispredictions of one traced run).
   value  device-timed processing loop (CUDA events on the engine's compute
          stream, from after the first generate to the end of the loop, the
          reference's t_processing convention)
