@@ -122,7 +122,8 @@ typedef struct sgw_engine_opts {
   uint32_t inner_batch;    /* async inner iterations launched per host check  */
   uint32_t tile_degree_max;/* sources above this degree go to the chunk list  */
   uint32_t chunk_edges;    /* edges per chunk-list item (multiple of 32)      */
-  uint32_t gather_ctas;    /* CTAs of the gather kernel, 0 = 2 per SM          */
+  uint32_t gather_ctas;    /* CTAs of the gather kernel, 0 = 2 per SM (3 per SM
+                              under the learned policy)                      */
   uint32_t num_buffers;    /* device edge buffers sharing the budget, 0 = 2
                               (1 with SGW_OPT_NO_OVERLAP), at most 8          */
   /* Learned policy, async mode: a range whose predicted active-edge fraction
