@@ -99,8 +99,9 @@ def build_apps(verbose=False, force=False) -> Path:
     if force or not _newer([main], deps):
         _run_parallel([["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", src, "-o", main,
                         f"-L{LIBDIR}", "-lsubwaygb", f"-Wl,-rpath,{LIBDIR}"]], verbose)
-    # one name per reference binary; the app picks algorithm and mode from argv[0]
-    for a in APPS:
+    # one name per reference binary (and tools/converter); the program picks
+    # what to do from argv[0]
+    for a in APPS + ["converter"]:
         link = BINDIR / a
         if link.is_symlink() or link.exists():
             link.unlink()

@@ -10,13 +10,20 @@
 // Extra flags: --budget BYTES (device-memory budget), --inner N (async inner
 // iterations per partition visit, 0 = until converged), --stats FILE (JSON),
 // --scheduler MODEL (learned scheduling policy with this network file; the
-// answers are the same, the schedule and the bytes moved change).
+// answers are the same, the schedule and the bytes moved change), --precision
+// DIGITS (significant digits of PageRank values in the --output file; the
+// reference writes 6, 9 round-trips every float exactly).
+//
+// Invoked as `converter`, it is the reference's tools/converter: one argument,
+// a .el or .wel file, written beside it as .bcsr or .bwcsr
+// (tools/converter.cpp:20-172), through the library's parallel text reader.
 
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <sys/time.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -30,6 +37,7 @@ struct Args {
   int device = 0;
   unsigned long long budget = 0;
   unsigned inner = 0;
+  int precision = 6;
   bool has_output = false;
 };
 
@@ -44,6 +52,7 @@ std::string help(bool can_source) {
   s += "\n    [--inner]: Async inner iterations per partition visit (default: 0 = until converged)";
   s += "\n    [--stats]: Write run statistics as JSON to this file";
   s += "\n    [--scheduler]: Learned scheduling with this model file (e.g. subway_gb300/models/sched_mlp.bin)";
+  s += "\n    [--precision]: Significant digits of float results in the output file (default: 6)";
   s += "\n\n";
   return s;
 }
@@ -72,6 +81,7 @@ Args parse(int argc, char **argv, bool can_source) {
     else if (!strcmp(k, "--inner")) a.inner = (unsigned)strtoul(v, nullptr, 10);
     else if (!strcmp(k, "--stats")) a.stats = v;
     else if (!strcmp(k, "--scheduler")) a.scheduler = v;
+    else if (!strcmp(k, "--precision")) a.precision = std::max(1, std::min(17, atoi(v)));
     else {
       std::string m = std::string("\nThere was an error parsing command line argument <") + k + ">\n";
       usage_exit(can_source, m.c_str());
@@ -114,16 +124,39 @@ void save_u32(const std::string &path, const std::vector<unsigned> &v) {
   printf("Done saving.\n");
 }
 
-void save_f32(const std::string &path, const std::vector<float> &v) {
+void save_f32(const std::string &path, const std::vector<float> &v, int digits) {
   printf("Saving the results into %s ...... ", path.c_str());
   fflush(stdout);
   FILE *f = fopen(path.c_str(), "w");
   if (!f) die(SGW_EIO, "SaveResults");
   std::vector<char> buf(1 << 22);
   setvbuf(f, buf.data(), _IOFBF, buf.size());
-  for (size_t i = 0; i < v.size(); ++i) fprintf(f, "%zu %g\n", i, (double)v[i]);
+  for (size_t i = 0; i < v.size(); ++i) fprintf(f, "%zu %.*g\n", i, digits, (double)v[i]);
   fclose(f);
   printf(" Completed.\n");
+}
+
+// tools/converter: messages and exit codes as tools/converter.cpp:22-25,167-170.
+int convert(int argc, char **argv) {
+  if (argc != 2) {
+    printf("\nThere was an error parsing command line arguments\n");
+    return 0;
+  }
+  std::string in = argv[1];
+  size_t dot = in.find_last_of('.');
+  std::string ext = dot == std::string::npos ? "" : in.substr(dot + 1);
+  if (ext != "el" && ext != "wel") {
+    printf("\nInput file format is not supported.\n");
+    return 0;
+  }
+  sgw_graph *g = nullptr;
+  int st = sgw_graph_load(in.c_str(), &g);
+  if (st != SGW_OK) die(st, "converter");
+  std::string outp = in.substr(0, dot + 1) + (ext == "el" ? "bcsr" : "bwcsr");
+  st = sgw_graph_save(g, outp.c_str());
+  sgw_graph_free(g);
+  if (st != SGW_OK) die(st, "converter");
+  return 0;
 }
 
 }  // namespace
@@ -132,6 +165,7 @@ int main(int argc, char **argv) {
   std::string name = argv[0];
   size_t slash = name.find_last_of('/');
   if (slash != std::string::npos) name = name.substr(slash + 1);
+  if (name == "converter") return convert(argc, argv);
   size_t dash = name.find('-');
   std::string algo_s = name.substr(0, dash), mode_s = dash == std::string::npos ? "" : name.substr(dash + 1);
   int algo = algo_s == "bfs" ? SGW_BFS : algo_s == "sssp" ? SGW_SSSP : algo_s == "sswp" ? SGW_SSWP
@@ -214,7 +248,7 @@ int main(int argc, char **argv) {
   if (algo == SGW_PR) print_results(vf, shown);
   else print_results(vu, shown);
   if (a.has_output) {
-    if (algo == SGW_PR) save_f32(a.output, vf);
+    if (algo == SGW_PR) save_f32(a.output, vf, a.precision);
     else save_u32(a.output, vu);
   }
   if (!a.stats.empty()) {

@@ -10,6 +10,10 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <atomic>
@@ -303,49 +307,64 @@ static std::string extension_of(const char *path) {
   return s.substr(dot + 1);
 }
 
+// Reads [off, off + bytes) of fd into dst with T threads, each issuing pread
+// calls of at most 64 MiB on its own contiguous slice.  Returns false on a short
+// read or an I/O error.
+static bool pread_parallel(int fd, char *dst, size_t bytes, off_t off) {
+  const size_t kPiece = size_t(64) << 20;
+  const int T = (int)std::max<size_t>(1, std::min<size_t>(omp_get_max_threads(), (bytes >> 23) + 1));
+  int bad = 0;
+#pragma omp parallel num_threads(T) reduction(| : bad)
+  {
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    size_t lo = bytes * t / nt, hi = bytes * (t + 1) / nt;
+    while (lo < hi && !bad) {
+      ssize_t r = pread(fd, dst + lo, std::min(hi - lo, kPiece), off + (off_t)lo);
+      if (r <= 0) bad = 1;
+      else lo += size_t(r);
+    }
+  }
+  return !bad;
+}
+
 static int load_binary(const char *path, int weighted, sgw_graph **out) {
-  FILE *f = fopen(path, "rb");
-  if (!f) return fail(SGW_EIO, "cannot open %s", path);
+  int fd = open(path, O_RDONLY);
+  if (fd < 0) return fail(SGW_EIO, "cannot open %s", path);
   uint32_t hdr[2];
-  if (fread(hdr, sizeof(uint32_t), 2, f) != 2) {
-    fclose(f);
+  struct stat sb;
+  if (pread(fd, hdr, sizeof(hdr), 0) != (ssize_t)sizeof(hdr) || fstat(fd, &sb) != 0) {
+    close(fd);
     return fail(SGW_EFORMAT, "%s: truncated header", path);
   }
   uint32_t n = hdr[0], m = hdr[1];
-  if (n == 0) { fclose(f); return fail(SGW_EFORMAT, "%s: zero vertices", path); }
+  if (n == 0) { close(fd); return fail(SGW_EFORMAT, "%s: zero vertices", path); }
   const uint32_t esz = weighted ? 8 : 4;
-  fseek(f, 0, SEEK_END);
-  long long fsz = ftell(f);
+  long long fsz = (long long)sb.st_size;
   long long want = 8LL + 4LL * n + (long long)m * esz;
   if (fsz != want) {
-    fclose(f);
+    close(fd);
     return fail(SGW_EFORMAT, "%s: size %lld, expected %lld for n=%u m=%u", path,
                 fsz, want, n, m);
   }
-  fseek(f, 8, SEEK_SET);
   sgw_graph *g = nullptr;
   int st = graph_alloc(n, m, weighted, &g);
-  if (st != SGW_OK) { fclose(f); return st; }
-  size_t got = fread(g->node_pointer, sizeof(uint32_t), n, f);
+  if (st != SGW_OK) { close(fd); return st; }
+  // [u32 n][u32 m][u32 nodePointer x n][edge x m] (graph.cu:43-51); the
+  // sentinel nodePointer[n] = m is implied
+  bool ok = pread_parallel(fd, (char *)g->node_pointer, sizeof(uint32_t) * size_t(n), 8) &&
+            pread_parallel(fd, (char *)g->edges, size_t(m) * esz, 8 + 4 * (off_t)n);
+  close(fd);
   g->node_pointer[n] = m;
-  // large sequential read in 256 MiB pieces
-  size_t total = size_t(m) * esz, done = 0;
-  char *dst = (char *)g->edges;
-  while (got == n && done < total) {
-    size_t piece = std::min(total - done, size_t(256) << 20);
-    size_t r = fread(dst + done, 1, piece, f);
-    if (r == 0) break;
-    done += r;
-  }
-  fclose(f);
-  if (got != n || done != total) {
+  if (!ok) {
     sgw_graph_free(g);
     return fail(SGW_EFORMAT, "%s: truncated body", path);
   }
   // validate: monotone pointers within [0, m], endpoints < n
   int bad = 0;
-  for (uint32_t v = 0; v < n && !bad; ++v)
-    if (g->node_pointer[v] > g->node_pointer[v + 1]) bad = 1;
+  const uint32_t *np = g->node_pointer;
+#pragma omp parallel for reduction(| : bad)
+  for (int64_t v = 0; v < (int64_t)n; ++v)
+    if (np[v] > np[v + 1]) bad |= 1;
   if (!bad) {
     const uint32_t *ed = (const uint32_t *)g->edges;
     const size_t stride = esz / 4;
@@ -356,64 +375,188 @@ static int load_binary(const char *path, int weighted, sgw_graph **out) {
   if (bad) {
     sgw_graph_free(g);
     return fail(SGW_EFORMAT, "%s: %s", path,
-                bad == 1 ? "node pointers not monotone" : "edge endpoint out of range");
+                (bad & 1) ? "node pointers not monotone" : "edge endpoint out of range");
   }
   *out = g;
   return SGW_OK;
 }
 
-static int load_text(const char *path, int weighted, sgw_graph **out) {
-  FILE *f = fopen(path, "rb");
-  if (!f) return fail(SGW_EIO, "cannot open %s", path);
+// Text edge lists: one "src dst" (.el) or "src dst w" (.wel) line per edge,
+// decimal u32 values separated by blanks (graph.cu:65-82, 120-137).  Blank
+// lines and lines starting with '#' or '%' are skipped; anything after the
+// last value of a line is ignored.  n = max id + 1 (graph.cu:85) and rows keep
+// file order, as the reference's counting sort does (graph.cu:92-113).
+//
+// The file is mapped and cut into one piece per thread at line starts; the
+// threads parse their pieces, count degrees with relaxed atomics, and then
+// place edges, each thread owning a vertex range of about m / T edges and
+// walking all pieces in file order, so the result does not depend on the
+// thread count.
+struct TextPiece {
   std::vector<uint32_t> src, dst, w;
-  char line[512];
-  uint64_t max_id = 0;
-  bool any = false;
-  while (fgets(line, sizeof(line), f)) {
-    char *p = line;
-    while (*p == ' ' || *p == '\t') ++p;
-    if (*p == '\n' || *p == '\r' || *p == 0 || *p == '#' || *p == '%') continue;
-    char *e1 = nullptr, *e2 = nullptr, *e3 = nullptr;
-    unsigned long long s = strtoull(p, &e1, 10);
-    if (e1 == p) { fclose(f); return fail(SGW_EFORMAT, "%s: bad line '%s'", path, line); }
-    unsigned long long d = strtoull(e1, &e2, 10);
-    if (e2 == e1) { fclose(f); return fail(SGW_EFORMAT, "%s: bad line '%s'", path, line); }
-    unsigned long long ww = 0;
-    if (weighted) {
-      ww = strtoull(e2, &e3, 10);
-      if (e3 == e2) { fclose(f); return fail(SGW_EFORMAT, "%s: missing weight in '%s'", path, line); }
-    }
-    if (s >= 0xffffffffULL || d >= 0xffffffffULL || ww > 0xffffffffULL) {
-      fclose(f);
-      return fail(SGW_ERANGE, "%s: value out of u32 range", path);
-    }
-    src.push_back((uint32_t)s);
-    dst.push_back((uint32_t)d);
-    if (weighted) w.push_back((uint32_t)ww);
-    max_id = std::max<uint64_t>(max_id, std::max(s, d));
-    any = true;
+  uint32_t max_id = 0;
+  size_t bad_at = SIZE_MAX;  // offset of the first bad line
+  int bad_status = SGW_OK;
+};
+
+static inline bool is_blank(char c) { return c == ' ' || c == '\t'; }
+
+// Parses one unsigned decimal at p (blanks skipped); false if there is none.
+static inline bool parse_u32(const char *&p, const char *end, uint64_t *v, bool *over) {
+  while (p < end && is_blank(*p)) ++p;
+  if (p == end || *p < '0' || *p > '9') return false;
+  uint64_t x = 0;
+  while (p < end && *p >= '0' && *p <= '9') {
+    x = x * 10 + uint64_t(*p - '0');
+    if (x > 0xffffffffULL) { *over = true; x = 0xffffffffULL + 1; }
+    ++p;
   }
-  fclose(f);
+  *v = x;
+  return true;
+}
+
+static void parse_piece(const char *base, size_t lo, size_t hi, int weighted, TextPiece &pc) {
+  const char *p = base + lo, *end = base + hi;
+  pc.src.reserve((hi - lo) / (weighted ? 10 : 7) + 16);
+  pc.dst.reserve(pc.src.capacity());
+  if (weighted) pc.w.reserve(pc.src.capacity());
+  while (p < end) {
+    const char *line = p;
+    const char *eol = (const char *)memchr(p, '\n', size_t(end - p));
+    if (!eol) eol = end;
+    while (p < eol && is_blank(*p)) ++p;
+    if (p < eol && *p != '\r' && *p != '#' && *p != '%') {
+      uint64_t s = 0, d = 0, w = 0;
+      bool over = false;
+      bool ok = parse_u32(p, eol, &s, &over) && parse_u32(p, eol, &d, &over) &&
+                (!weighted || parse_u32(p, eol, &w, &over));
+      if (!ok || over || s >= 0xffffffffULL || d >= 0xffffffffULL) {
+        pc.bad_at = size_t(line - base);
+        pc.bad_status = ok ? SGW_ERANGE : SGW_EFORMAT;
+        return;
+      }
+      pc.src.push_back((uint32_t)s);
+      pc.dst.push_back((uint32_t)d);
+      if (weighted) pc.w.push_back((uint32_t)w);
+      pc.max_id = std::max(pc.max_id, (uint32_t)std::max(s, d));
+    }
+    p = eol + 1;
+  }
+}
+
+static int load_text(const char *path, int weighted, sgw_graph **out) {
+  int fd = open(path, O_RDONLY);
+  if (fd < 0) return fail(SGW_EIO, "cannot open %s", path);
+  struct stat sb;
+  if (fstat(fd, &sb) != 0) { close(fd); return fail(SGW_EIO, "cannot stat %s", path); }
+  const size_t size = (size_t)sb.st_size;
+  if (size == 0) { close(fd); return fail(SGW_EFORMAT, "%s: no edges", path); }
+  void *map = mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
+  close(fd);
+  if (map == MAP_FAILED) return fail(SGW_EIO, "cannot map %s", path);
+  madvise(map, size, MADV_SEQUENTIAL);
+  const char *base = (const char *)map;
+
+  const int T = (int)std::max<size_t>(1, std::min<size_t>(omp_get_max_threads(), size / (1 << 20) + 1));
+  std::vector<size_t> cut(size_t(T) + 1);
+  for (int t = 0; t <= T; ++t) {
+    size_t c = size * size_t(t) / size_t(T);
+    if (t > 0 && t < T)
+      while (c < size && base[c - 1] != '\n') ++c;  // first line starting at or after c
+    cut[t] = c;
+  }
+  std::vector<TextPiece> pcs(T);
+#pragma omp parallel for schedule(static, 1) num_threads(T)
+  for (int t = 0; t < T; ++t)
+    if (cut[t] < cut[t + 1]) parse_piece(base, cut[t], cut[t + 1], weighted, pcs[t]);
+
+  for (int t = 0; t < T; ++t)  // pieces in file order: the first bad line wins
+    if (pcs[t].bad_status != SGW_OK) {
+      const char *line = base + pcs[t].bad_at;
+      const char *eol = (const char *)memchr(line, '\n', size - pcs[t].bad_at);
+      int len = (int)std::min<size_t>(eol ? size_t(eol - line) : size - pcs[t].bad_at, 200);
+      std::string text(line, size_t(len));
+      munmap(map, size);
+      return pcs[t].bad_status == SGW_ERANGE
+                 ? fail(SGW_ERANGE, "%s: value out of u32 range in '%s'", path, text.c_str())
+                 : fail(SGW_EFORMAT, "%s: bad line '%s'", path, text.c_str());
+    }
+  munmap(map, size);
+
+  uint64_t m = 0;
+  uint32_t max_id = 0;
+  bool any = false;
+  for (const TextPiece &pc : pcs) {
+    m += pc.src.size();
+    if (!pc.src.empty()) { any = true; max_id = std::max(max_id, pc.max_id); }
+  }
   if (!any) return fail(SGW_EFORMAT, "%s: no edges", path);
-  uint32_t n = (uint32_t)(max_id + 1);  // num_nodes = max + 1 (graph.cu:85)
-  uint64_t m = src.size();
+  const uint32_t n = max_id + 1;
   sgw_graph *g = nullptr;
   int st = graph_alloc(n, m, weighted, &g);
   if (st != SGW_OK) return st;
-  // stable counting sort by source: file order within a row (graph.cu:92-113)
-  std::vector<uint32_t> cur(size_t(n) + 1, 0);
-  for (uint64_t i = 0; i < m; ++i) cur[src[i]]++;
-  uint32_t acc = 0;
-  for (uint32_t v = 0; v < n; ++v) { g->node_pointer[v] = acc; uint32_t c = cur[v]; cur[v] = acc; acc += c; }
-  g->node_pointer[n] = acc;
+  uint32_t *np = g->node_pointer;
+
+  // degrees, then an exclusive prefix in T blocks
+#pragma omp parallel for num_threads(T)
+  for (int64_t v = 0; v <= (int64_t)n; ++v) np[v] = 0;
+#pragma omp parallel for schedule(static, 1) num_threads(T)
+  for (int t = 0; t < T; ++t)
+    for (uint32_t s : pcs[t].src) __atomic_fetch_add(&np[s], 1u, __ATOMIC_RELAXED);
+  std::vector<uint64_t> block(size_t(T) + 1, 0);
+#pragma omp parallel num_threads(T)
+  {
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    const uint64_t lo = uint64_t(n) * t / nt, hi = uint64_t(n) * (t + 1) / nt;
+    uint64_t acc = 0;
+    for (uint64_t v = lo; v < hi; ++v) acc += np[v];
+    block[t + 1] = acc;
+#pragma omp barrier
+#pragma omp single
+    for (int k = 1; k <= nt; ++k) block[k] += block[k - 1];
+    uint64_t run = block[t];
+    for (uint64_t v = lo; v < hi; ++v) {
+      uint32_t c = np[v];
+      np[v] = (uint32_t)run;
+      run += c;
+    }
+  }
+  np[n] = (uint32_t)m;
+
+  // placement: thread j owns the sources whose rows start in its 1/T of the
+  // edge range and scans every piece in file order, keeping rows stable
+  std::vector<uint32_t> cur(np, np + n);
   uint32_t *ed = (uint32_t *)g->edges;
-  for (uint64_t i = 0; i < m; ++i) {
-    uint32_t pos = cur[src[i]]++;
-    if (weighted) { ed[2 * size_t(pos)] = dst[i]; ed[2 * size_t(pos) + 1] = w[i]; }
-    else ed[pos] = dst[i];
+#pragma omp parallel num_threads(T)
+  {
+    const int j = omp_get_thread_num(), nt = omp_get_num_threads();
+    const uint32_t e_lo = (uint32_t)(m * j / nt), e_hi = (uint32_t)(m * (j + 1) / nt);
+    // first vertex whose row starts at or after e_lo / e_hi
+    const uint32_t v_lo = j == 0 ? 0 : (uint32_t)(std::lower_bound(np, np + n, e_lo) - np);
+    const uint32_t v_hi = j == nt - 1 ? n : (uint32_t)(std::lower_bound(np, np + n, e_hi) - np);
+    if (v_lo < v_hi)
+      for (const TextPiece &pc : pcs) {
+        const size_t k = pc.src.size();
+        for (size_t i = 0; i < k; ++i) {
+          const uint32_t s = pc.src[i];
+          if (s < v_lo || s >= v_hi) continue;
+          const uint32_t pos = cur[s]++;
+          if (weighted) { ed[2 * size_t(pos)] = pc.dst[i]; ed[2 * size_t(pos) + 1] = pc.w[i]; }
+          else ed[pos] = pc.dst[i];
+        }
+      }
   }
   *out = g;
   return SGW_OK;
+}
+
+// Writes x in decimal at q and returns the end.
+static inline char *put_u32(char *q, uint32_t x) {
+  char d[10];
+  int k = 0;
+  do { d[k++] = char('0' + x % 10); x /= 10; } while (x);
+  while (k) *q++ = d[--k];
+  return q;
 }
 
 }  // namespace sgw
@@ -538,11 +681,43 @@ int sgw_graph_save(const sgw_graph *g, const char *path) {
       }
     }
   } else {
-    for (uint32_t v = 0; ok && v < g->n; ++v)
-      for (uint32_t i = g->node_pointer[v]; ok && i < g->node_pointer[v + 1]; ++i) {
-        if (want_w) ok = fprintf(f, "%u %u %u\n", v, ed[size_t(i) * stride], ed[size_t(i) * stride + 1]) > 0;
-        else ok = fprintf(f, "%u %u\n", v, ed[size_t(i) * stride]) > 0;
+    // text: vertex blocks of about 2^24 edges, each formatted by T threads
+    // into their own buffers and written in order
+    const int T = omp_get_max_threads();
+    std::vector<std::string> bufs(T);
+    uint32_t v0 = 0;
+    while (ok && v0 < g->n) {
+      const uint32_t e0 = g->node_pointer[v0];
+      uint32_t v1 = (uint32_t)(std::upper_bound(g->node_pointer + v0, g->node_pointer + g->n,
+                                                 uint64_t(e0) + (1u << 24)) - g->node_pointer);
+      v1 = std::max(v1, v0 + 1);
+      const uint64_t span = uint64_t(g->node_pointer[v1]) - e0;
+#pragma omp parallel num_threads(T)
+      {
+        const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+        const uint32_t lo_e = (uint32_t)(e0 + span * t / nt), hi_e = (uint32_t)(e0 + span * (t + 1) / nt);
+        std::string &b = bufs[t];
+        b.clear();
+        b.reserve(size_t(hi_e - lo_e) * (want_w ? 24 : 20));
+        // the vertex whose row holds edge lo_e
+        uint32_t v = (uint32_t)(std::upper_bound(g->node_pointer + v0, g->node_pointer + v1, lo_e) -
+                                g->node_pointer) - 1;
+        char tmp[40];
+        for (uint32_t i = lo_e; i < hi_e; ++i) {
+          while (g->node_pointer[v + 1] <= i) ++v;
+          char *q = tmp;
+          q = put_u32(q, v);
+          *q++ = ' ';
+          q = put_u32(q, ed[size_t(i) * stride]);
+          if (want_w) { *q++ = ' '; q = put_u32(q, ed[size_t(i) * stride + 1]); }
+          *q++ = '\n';
+          b.append(tmp, size_t(q - tmp));
+        }
       }
+      for (int t = 0; ok && t < T; ++t)
+        ok = bufs[t].empty() || fwrite(bufs[t].data(), 1, bufs[t].size(), f) == bufs[t].size();
+      v0 = v1;
+    }
   }
   if (fclose(f) != 0) ok = false;
   return ok ? SGW_OK : fail(SGW_EIO, "write failed for %s", path);

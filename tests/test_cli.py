@@ -45,6 +45,46 @@ def test_missing_file_fails_without_a_gpu_call(bindir, tmp_path):
     assert p.returncode != 0 and "cannot open" in p.stderr
 
 
+README_EL = "0 1\n0 3\n2 3\n1 2\n"  # the reference README's example graph
+README_WEL = "0 1 26\n0 3 33\n2 3 40\n1 2 10\n"
+
+
+def test_converter_writes_the_reference_binary_layout(bindir, tmp_path):
+    """tools/converter.cpp:20-172: g.el -> g.bcsr, g.wel -> g.bwcsr, laid out
+    [n][m][nodePointer x n][edges x m] with rows in file order."""
+    (tmp_path / "Graph.el").write_text(README_EL)
+    (tmp_path / "Graph.wel").write_text(README_WEL)
+    for name in ("Graph.el", "Graph.wel"):
+        p = _run(bindir, "converter", tmp_path / name)
+        assert p.returncode == 0, p.stderr
+    raw = np.frombuffer((tmp_path / "Graph.bcsr").read_bytes(), np.uint32)
+    assert raw.tolist() == [4, 4, 0, 2, 3, 4, 1, 3, 2, 3]
+    raw = np.frombuffer((tmp_path / "Graph.bwcsr").read_bytes(), np.uint32)
+    assert raw.tolist() == [4, 4, 0, 2, 3, 4, 1, 26, 3, 33, 2, 10, 3, 40]
+
+
+def test_converter_argument_errors_exit_zero(bindir, tmp_path):
+    p = _run(bindir, "converter")
+    assert p.returncode == 0 and "There was an error parsing command line arguments" in p.stdout
+    p = _run(bindir, "converter", tmp_path / "a.el", tmp_path / "b.el")
+    assert p.returncode == 0 and "There was an error parsing command line arguments" in p.stdout
+    (tmp_path / "g.txt").write_text(README_EL)
+    p = _run(bindir, "converter", tmp_path / "g.txt")
+    assert p.returncode == 0 and "Input file format is not supported." in p.stdout
+    p = _run(bindir, "converter", tmp_path / "missing.el")
+    assert p.returncode != 0 and "cannot open" in p.stderr
+
+
+def test_converter_large_file_round_trip(native, bindir, tmp_path):
+    g = native.Graph.rmat(14, 16, seed=21, weighted=True, wmax=64)
+    g.save(tmp_path / "r.wel")
+    p = _run(bindir, "converter", tmp_path / "r.wel")
+    assert p.returncode == 0, p.stderr
+    h = native.Graph.load(tmp_path / "r.bwcsr")
+    assert h.m == g.m and np.array_equal(h.edges, g.edges)
+    assert np.array_equal(h.node_pointer, g.node_pointer[: h.n + 1])
+
+
 def _write(gpu, tmp_path, weighted):
     g = gpu.Graph.rmat(12, 8, seed=77, weighted=weighted, wmax=64)
     path = tmp_path / ("g.bwcsr" if weighted else "g.bcsr")
@@ -96,3 +136,26 @@ def test_app_learned_scheduler_same_answers(gpu, orc, bindir, tmp_path):
     assert re.search(r"Inner Iterations? in Global Iteration \d+, Range \d+", p.stdout)
     rows = np.loadtxt(out)
     assert np.array_equal(rows[:, 1].astype(np.uint64), orc.run("sssp", g.node_pointer, g.edges, 1).astype(np.uint64))
+
+
+@pytest.mark.gpu
+def test_pr_output_precision(gpu, orc, bindir, tmp_path):
+    """--precision 9 writes every PageRank value so that it reads back as the
+    same float32; the default keeps the reference's 6 digits."""
+    g, path = _write(gpu, tmp_path, False)
+    budget = 36 * g.n + 64 * 1024 + 4000 * 8
+    for digits in (6, 9):
+        out = tmp_path / f"pr{digits}.txt"
+        args = ["--input", path, "--output", out, "--budget", budget]
+        if digits != 6:
+            args += ["--precision", digits]
+        p = _run(bindir, "pr-sync", *args)
+        assert p.returncode == 0, p.stderr
+        vals = [ln.split()[1] for ln in out.read_text().splitlines()]
+        sig = max(len(v.split("e")[0].replace(".", "").lstrip("0")) for v in vals)
+        assert sig == digits
+        x = np.array(vals, np.float64).astype(np.float32)
+        if digits == 9:
+            assert all(f"{float(v):.9g}" == s for v, s in zip(x, vals))
+        ref, _ = orc.pagerank(g.node_pointer, g.ends)
+        assert np.max(np.abs(x - ref) / ref) < 1e-4

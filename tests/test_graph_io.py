@@ -138,3 +138,86 @@ def test_pick_sources(native):
     assert np.all(g.out_degree()[a] > 0)
     nv, ne = g.largest_wcc()
     assert nv > g.n // 4 and ne > g.m // 2
+
+
+def _reference_text_csr(text, weighted):
+    """The reference's text reader restated (graph.cu:65-113): n = max id + 1,
+    a counting sort by source that keeps file order within a row.  Blank and
+    comment lines are skipped, as this library documents."""
+    rows = []
+    for line in text.splitlines():
+        t = line.strip(" \t\r")
+        if not t or t[0] in "#%":
+            continue
+        f = t.split()
+        rows.append(tuple(int(x) for x in f[: 3 if weighted else 2]))
+    n = max(max(r[0], r[1]) for r in rows) + 1
+    order = sorted(range(len(rows)), key=lambda i: rows[i][0])  # stable
+    npt = np.zeros(n + 1, np.uint32)
+    np.add.at(npt, np.array([r[0] for r in rows]) + 1, 1)
+    npt = np.cumsum(npt).astype(np.uint32)
+    edges = np.array([rows[i][1:] for i in order], np.uint32)
+    return n, npt, edges if weighted else edges[:, 0]
+
+
+def _messy_text(rng, m, n, weighted):
+    lines = ["# comment", "% another comment"]
+    for k in range(m):
+        s, d = int(rng.integers(n)), int(rng.integers(n))
+        sep = "\t" if k % 7 == 0 else " "
+        line = f"{s}{sep}{d}" + (f" {int(rng.integers(1, 2**32))}" if weighted else "")
+        if k % 11 == 0:
+            line = "  " + line + " trailing"
+        if k % 13 == 0:
+            line += "\r"
+        lines.append(line)
+        if k % 97 == 0:
+            lines.append("")
+    return "\n".join(lines)  # no newline after the last line
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_text_load_matches_reference_reader(native, tmp_path, weighted):
+    """Several pieces per file (> 1 MiB), duplicates, unsorted rows, tabs,
+    CRLF, comments, blank lines and a missing final newline."""
+    rng = np.random.default_rng(11 + weighted)
+    text = _messy_text(rng, 150_000, 5000, weighted)
+    assert len(text) > (1 << 20)
+    p = tmp_path / ("g.wel" if weighted else "g.el")
+    p.write_text(text)
+    n, npt, edges = _reference_text_csr(text, weighted)
+    g = native.Graph.load(p)
+    assert (g.n, g.m) == (n, len(edges))
+    assert np.array_equal(g.node_pointer, npt)
+    assert np.array_equal(g.edges if weighted else g.ends, edges)
+
+
+def test_text_io_independent_of_thread_count(tmp_path):
+    rng = np.random.default_rng(5)
+    (tmp_path / "g.wel").write_text(_messy_text(rng, 200_000, 30_000, True))
+    code = ("import sys, hashlib; sys.path.insert(0, %r); from subway_gb300 import native as N; "
+            "g=N.Graph.load(sys.argv[1]); g.save(sys.argv[2]); h=hashlib.sha256(); "
+            "h.update(g.node_pointer.tobytes()); h.update(g.edges.tobytes()); "
+            "h.update(open(sys.argv[2], 'rb').read()); print(h.hexdigest())" % str(ROOT))
+    outs = []
+    for t in ("1", "3", "8"):
+        env = dict(os.environ, OMP_NUM_THREADS=t)
+        outs.append(subprocess.run([sys.executable, "-c", code, str(tmp_path / "g.wel"),
+                                    str(tmp_path / f"out{t}.wel")], env=env, capture_output=True,
+                                   text=True, check=True).stdout.strip())
+    assert outs[0] == outs[1] == outs[2]
+
+
+def test_text_errors_name_the_first_bad_line(native, tmp_path):
+    good = "".join(f"{i} {i + 1}\n" for i in range(120_000))
+    (tmp_path / "bad.el").write_text(good + "7 x\n" + good + "1 2 3\nq\n")
+    with pytest.raises(native.SgwError) as e:
+        native.Graph.load(tmp_path / "bad.el")
+    assert e.value.status == -3 and "'7 x'" in str(e.value)
+    (tmp_path / "big.el").write_text(good + "4294967295 1\n")
+    with pytest.raises(native.SgwError) as e:
+        native.Graph.load(tmp_path / "big.el")
+    assert e.value.status == -9  # SGW_ERANGE: ids must stay below 2^32 - 1
+    (tmp_path / "empty.el").write_text("# only a comment\n\n")
+    with pytest.raises(native.SgwError):
+        native.Graph.load(tmp_path / "empty.el")
