@@ -1,7 +1,7 @@
 """Compiles the CPU oracle (sgw_oracle.c) into oracle/build/libsgw_oracle.so.
 
-Test infrastructure: the library is the checker for the tests and the CPU
-baseline of the benchmark, never part of the engine.
+Test infrastructure: the library gives the tests their expected answers and
+the benchmark its CPU baseline; it is never part of the engine.
 """
 from __future__ import annotations
 

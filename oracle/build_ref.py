@@ -4,8 +4,8 @@ TEST AND BASELINE INFRASTRUCTURE.  Outputs only under oracle/_ref/ (git-ignored)
 
   oracle/_ref/src/        the reference's shared/ and subway/ sources, copied
                           verbatim from the reference tree when it is present
-                          (this container), so that the GPU machine, which has no
-                          reference tree, can compile them too
+                          (this container), so that a GPU machine without the
+                          reference tree can compile them too
   oracle/_ref/bin/        the ten apps as shipped (bfs-sync ... pr-async)
   oracle/_ref/bin_fixed/  the same apps with the host-gather chunk size
                           rounded up (shared/subgraph_generator.cu:75 divides

@@ -1,7 +1,7 @@
 /*
  * sgw_oracle.c — CPU oracle for the Subway hot path.  TEST INFRASTRUCTURE:
  * only the tests, the smoke check and the benchmark's CPU-baseline leg load
- * this library, as the checker and as the reported CPU baseline; the engine
+ * this library, for expected answers and as the reported CPU baseline; the engine
  * never calls it.
  *
  * Two groups of functions:

@@ -192,7 +192,7 @@ int check_ctl_error(sgw_engine *e) {
 }
 
 // Whole-range streaming moves records by DMA from the transfer copy.  On
-// some boxes of one pool the learned policy's transfers ran at half their
+// some GB300 machines the learned policy's transfers ran at half their
 // usual rate while the plain policy's gathers did not, so the engine times a
 // few DMA copies at creation (and, when profiling, the streamed copies of
 // every run, in prof_collect); the learned policy streams whole ranges only

@@ -24,7 +24,7 @@ namespace sgw {
 int fail(int status, const char *fmt, ...);
 void clear_error();
 
-// Page-aligned host allocation (64 KiB granularity, the GPU machine's page size),
+// Page-aligned host allocation (64 KiB granularity, the page size of Arm GB300 hosts),
 // suitable for cudaHostRegister.  Returns nullptr on failure.
 void *host_alloc(size_t bytes, size_t *rounded);
 void host_free(void *p);

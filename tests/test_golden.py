@@ -1,7 +1,7 @@
 """The oracle against the Subway reference's own outputs.
 
 tests/golden/ref_rmat13.npz holds every app's output from the reference build
-(as shipped and with the host-gather chunk fix), run on the GPU machine by
+(as shipped and with the host-gather chunk fix), run on a GB300 by
 tests/golden/make_golden.py on a seeded R-MAT scale-13 graph; the graph is
 regenerated here and checked against the stored digest first."""
 import hashlib
