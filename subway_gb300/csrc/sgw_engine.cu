@@ -455,11 +455,19 @@ int launch_generate(sgw_engine *e, int consume) {
   CK(cudaMemsetAsync(&e->d_ctl->num_seen, 0, sizeof(uint32_t), e->s_comp));
   size_t slot = 0;
   TRY(prof_begin(e, K_GENERATE, e->s_comp, &slot));
-  if (e->fam == FAM_PR) k_generate<true><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
-  else k_generate_v<<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  if (e->fam == FAM_PR) {
+    k_generate<true><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+    e->stats.launches += 1;
+  } else {
+    k_generate_count<<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+    CK(cudaGetLastError());
+    k_generate_scan<<<1, kGenScanThreads, 0, e->s_comp>>>(a);
+    CK(cudaGetLastError());
+    k_generate_write<<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+    e->stats.launches += 3;
+  }
   CK(cudaGetLastError());
   TRY(prof_end(e, e->s_comp, slot));
-  e->stats.launches += 1;
   e->stats.generate_launches += 1;
   e->parts_valid = false;
   return SGW_OK;

@@ -2,17 +2,19 @@
 //
 // Hot path per global iteration (reference: shared/subgraph_generator.cu:
 // 128-204 and subway/*-{sync,async}.cu):
-//   k_generate   activeness + single-pass decoupled-lookback scan + compaction
-//                into the active queue (replaces prePrefix, thrust::reduce,
-//                two thrust::exclusive_scan, makeQueue, makeActiveNodesPointer)
+//   k_generate_count / _scan / _write (BFS, SSSP, SSWP, CC) and k_generate
+//                (PageRank; single-pass decoupled-lookback scan): activeness,
+//                scan and compaction into the active queue (replaces
+//                prePrefix, thrust::reduce, two thrust::exclusive_scan,
+//                makeQueue, makeActiveNodesPointer)
 //   k_plan       greedy partition boundaries on the device (Partitioner)
 //   k_gather_v   active-edge gather from the engine's mapped pinned transfer
 //                copy of the edges into an HBM edge buffer, 16-byte reads
 //                (replaces the host std::thread copy dynamic<E>); k_gather
 //                is the one-record-per-thread form
-//   k_relax_tile CTA-cooperative expansion of a tile of frontier sources
-//                staged in shared memory (bfs/sssp/sswp/cc kernels, sync and
-//                async forms)
+//   k_relax_warp warp-cooperative expansion of 32 frontier sources at a time
+//                (bfs/sssp/sswp/cc kernels, sync and async forms); k_relax_tile
+//                the CTA-tile form staged in shared memory
 //   k_relax_chunks warp-per-chunk expansion of high-degree sources
 // Learned policy only (no reference counterpart):
 //   k_select_*   value range, degree histogram and cut of the frontier when
@@ -381,164 +383,221 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
   }
 }
 
-// Integer-family generate with 16 consecutive vertices per lane: the lane
-// reads their labels as two 16-byte words and, only if one of them is
-// active, their 17 node pointers (and values, for the learned policy's
-// selection) as 16-byte words; per-lane counts and edge sums are scanned
-// within the warp, then across the CTA and the tiles exactly as in
-// k_generate, and each lane writes its queued vertices in order.  Same
-// results as k_generate<false>; the label, pointer and value arrays must be
-// 16-byte aligned (the engine's arena is).
+// Integer-family generate with 16 consecutive vertices per lane, in three
+// launches with no chain between CTAs: k_generate_count, k_generate_scan,
+// k_generate_write.  A lane reads its vertices' labels as two 16-byte words
+// and, only if one of them is active, their 17 node pointers (and values, for
+// the learned policy's selection) as 16-byte words.  The count pass stores
+// each 4096-vertex tile's (queued vertices, edges) total; one CTA turns the
+// totals into exclusive tile prefixes; the write pass recomputes the same
+// selection from the same labels and values, scans within the tile, writes
+// the queue and pointers in order and clears the consumed labels.  Labels
+// and values do not change between the passes (nothing else runs on the
+// stream in between), so both passes select the same vertices.  Same results
+// as k_generate<false>; the label, pointer and value arrays must be 16-byte
+// aligned (the engine's arena is).
+//
+// The single-pass form with a decoupled look-back (k_generate, kept for
+// PageRank and the allocation-free entry point) took 1.7-2x as long on
+// RMAT-24: with hundreds of tiles in flight the prefixes travel 32 tiles per
+// look-back step and every CTA of a wave waits for them, while the second
+// pass's labels and pointers come mostly from L2.
 constexpr uint32_t kGenVPerLane = 16;
-__global__ void __launch_bounds__(kGenThreads) k_generate_v(GenArgs a) {
-  __shared__ uint32_t s_tile;
-  __shared__ unsigned long long s_warp[kGenThreads / 32];
-  __shared__ unsigned long long s_prefix;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) s_tile = atomicAdd(&a.ctl->tile_ticket, 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  if (tile >= a.num_tiles) {  // stale ticket counter: refuse to index past the tiles
-    if (tid == 0) atomicExch(&a.ctl->error, 4u);
-    return;
-  }
-  const uint32_t v0 = tile * kGenTile + warp * (32 * kGenRounds) + lane * kGenVPerLane;
+
+struct GenLane {
+  uint32_t keepmask = 0, clearmask = 0, cnt = 0, edges = 0, seen = 0;
+  uint32_t l1w[4] = {0, 0, 0, 0}, l2w[4] = {0, 0, 0, 0};
+  uint32_t o[kGenVPerLane + 1];  // node pointers; a queued vertex's degree is o[k + 1] - o[k]
+};
+
+// Selection for the lane's 16 vertices starting at v0.
+__device__ __forceinline__ void gen_lane(const GenArgs &a, uint32_t v0, bool full, GenLane &L) {
   uint32_t sel_lo = 0, sel_hi = 0, sel_bin = 0;
   if (a.sel_mode & 2) {
     sel_lo = a.ctl->sel_lo;
     sel_hi = a.ctl->sel_hi;
     sel_bin = a.ctl->sel_bin;
   }
-  const bool full = v0 + kGenVPerLane <= a.n;
-  // activeness bytes of the lane's 16 vertices
-  uint32_t lw[4] = {0, 0, 0, 0}, l1w[4] = {0, 0, 0, 0}, l2w[4] = {0, 0, 0, 0};
   if (full) {
     const uint4 x = *reinterpret_cast<const uint4 *>(a.l1 + v0);
     const uint4 y = *reinterpret_cast<const uint4 *>(a.l2 + v0);
-    l1w[0] = x.x; l1w[1] = x.y; l1w[2] = x.z; l1w[3] = x.w;
-    l2w[0] = y.x; l2w[1] = y.y; l2w[2] = y.z; l2w[3] = y.w;
+    L.l1w[0] = x.x; L.l1w[1] = x.y; L.l1w[2] = x.z; L.l1w[3] = x.w;
+    L.l2w[0] = y.x; L.l2w[1] = y.y; L.l2w[2] = y.z; L.l2w[3] = y.w;
   } else {
     for (uint32_t k = 0; k < kGenVPerLane; ++k)
       if (v0 + k < a.n) {
-        l1w[k / 4] |= (uint32_t)a.l1[v0 + k] << (8 * (k % 4));
-        l2w[k / 4] |= (uint32_t)a.l2[v0 + k] << (8 * (k % 4));
+        L.l1w[k / 4] |= (uint32_t)a.l1[v0 + k] << (8 * (k % 4));
+        L.l2w[k / 4] |= (uint32_t)a.l2[v0 + k] << (8 * (k % 4));
       }
   }
   uint32_t actmask = 0;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    lw[q] = l1w[q] | l2w[q];
+    const uint32_t lw = L.l1w[q] | L.l2w[q];
 #pragma unroll
     for (int b = 0; b < 4; ++b)
-      if ((lw[q] >> (8 * b)) & 0xffu) actmask |= 1u << (4 * q + b);
+      if ((lw >> (8 * b)) & 0xffu) actmask |= 1u << (4 * q + b);
   }
-  uint32_t keepmask = 0, clearmask = 0, cnt = 0, edges = 0;
-  uint32_t o[kGenVPerLane + 1];  // node pointers; a queued vertex's degree is o[k + 1] - o[k]
-  if (actmask) {
-    uint32_t val[kGenVPerLane];
-    if (full) {
+  L.seen = (uint32_t)__popc(actmask);
+  if (!actmask) return;
+  uint32_t val[kGenVPerLane];
+  if (full) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint4 p = __ldg(reinterpret_cast<const uint4 *>(a.off + v0) + q);
+      L.o[4 * q] = p.x; L.o[4 * q + 1] = p.y; L.o[4 * q + 2] = p.z; L.o[4 * q + 3] = p.w;
+    }
+    L.o[kGenVPerLane] = __ldg(&a.off[v0 + kGenVPerLane]);
+    if (a.sel_mode) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const uint4 p = __ldg(reinterpret_cast<const uint4 *>(a.off + v0) + q);
-        o[4 * q] = p.x; o[4 * q + 1] = p.y; o[4 * q + 2] = p.z; o[4 * q + 3] = p.w;
-      }
-      o[kGenVPerLane] = __ldg(&a.off[v0 + kGenVPerLane]);
-      if (a.sel_mode) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint4 p = reinterpret_cast<const uint4 *>(a.value + v0)[q];
-          val[4 * q] = p.x; val[4 * q + 1] = p.y; val[4 * q + 2] = p.z; val[4 * q + 3] = p.w;
-        }
-      }
-    } else {
-#pragma unroll
-      for (uint32_t k = 0; k <= kGenVPerLane; ++k) o[k] = (v0 + k <= a.n) ? __ldg(&a.off[v0 + k]) : 0u;
-#pragma unroll
-      for (uint32_t k = 0; k < kGenVPerLane; ++k) val[k] = (a.sel_mode && v0 + k < a.n) ? a.value[v0 + k] : 0u;
-    }
-#pragma unroll
-    for (uint32_t k = 0; k < kGenVPerLane; ++k) {
-      if (!((actmask >> k) & 1u)) continue;
-      uint32_t d = o[k + 1] - o[k];
-      bool drop = d == 0, defer = false;
-      if (a.sel_mode && !drop) {
-        if (!pushable(a.algo, val[k])) drop = (a.sel_mode & 1) != 0;
-        else if ((a.sel_mode & 2) && !selected(a.algo, val[k], sel_lo, sel_hi, sel_bin)) defer = true;
-      }
-      if (!defer && (a.consume || drop)) clearmask |= 1u << k;
-      if (!drop && !defer) {
-        keepmask |= 1u << k;
-        ++cnt;
-        edges += d;
+        const uint4 p = reinterpret_cast<const uint4 *>(a.value + v0)[q];
+        val[4 * q] = p.x; val[4 * q + 1] = p.y; val[4 * q + 2] = p.z; val[4 * q + 3] = p.w;
       }
     }
-    if (clearmask) {
-      uint32_t cw[4];
+  } else {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        cw[q] = 0;
+    for (uint32_t k = 0; k <= kGenVPerLane; ++k) L.o[k] = (v0 + k <= a.n) ? __ldg(&a.off[v0 + k]) : 0u;
 #pragma unroll
-        for (int b = 0; b < 4; ++b)
-          if ((clearmask >> (4 * q + b)) & 1u) cw[q] |= 0xffu << (8 * b);
-      }
-      if (full) {
-        *reinterpret_cast<uint4 *>(a.l1 + v0) = make_uint4(l1w[0] & ~cw[0], l1w[1] & ~cw[1], l1w[2] & ~cw[2], l1w[3] & ~cw[3]);
-        *reinterpret_cast<uint4 *>(a.l2 + v0) = make_uint4(l2w[0] & ~cw[0], l2w[1] & ~cw[1], l2w[2] & ~cw[2], l2w[3] & ~cw[3]);
-      } else {
-        for (uint32_t k = 0; k < kGenVPerLane; ++k)
-          if ((clearmask >> k) & 1u) { a.l1[v0 + k] = 0; a.l2[v0 + k] = 0; }
-      }
+    for (uint32_t k = 0; k < kGenVPerLane; ++k) val[k] = (a.sel_mode && v0 + k < a.n) ? a.value[v0 + k] : 0u;
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < kGenVPerLane; ++k) {
+    if (!((actmask >> k) & 1u)) continue;
+    uint32_t d = L.o[k + 1] - L.o[k];
+    bool drop = d == 0, defer = false;
+    if (a.sel_mode && !drop) {
+      if (!pushable(a.algo, val[k])) drop = (a.sel_mode & 1) != 0;
+      else if ((a.sel_mode & 2) && !selected(a.algo, val[k], sel_lo, sel_hi, sel_bin)) defer = true;
+    }
+    if (!defer && (a.consume || drop)) L.clearmask |= 1u << k;
+    if (!drop && !defer) {
+      L.keepmask |= 1u << k;
+      ++L.cnt;
+      L.edges += d;
     }
   }
-  const uint32_t seen = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(actmask));
-  const uint32_t incl_c = warp_incl_scan(cnt, lane);
-  const uint32_t incl_e = warp_incl_scan(edges, lane);
-  if (lane == 31) s_warp[warp] = ((unsigned long long)incl_c << 32) | incl_e;
-  if (lane == 0 && seen) atomicAdd(&a.ctl->num_seen, seen);
+}
+
+__global__ void __launch_bounds__(kGenThreads) k_generate_count(GenArgs a) {
+  __shared__ unsigned long long s_warp[kGenThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t v0 = tile * kGenTile + warp * (32 * kGenRounds) + lane * kGenVPerLane;
+  GenLane L;
+  if (v0 < a.n) gen_lane(a, v0, v0 + kGenVPerLane <= a.n, L);
+  const uint32_t seen = __reduce_add_sync(0xffffffffu, L.seen);
+  const uint32_t c = __reduce_add_sync(0xffffffffu, L.cnt);
+  const uint32_t e = __reduce_add_sync(0xffffffffu, L.edges);
+  if (lane == 0) {
+    s_warp[warp] = ((unsigned long long)c << 32) | e;
+    if (seen) atomicAdd(&a.ctl->num_seen, seen);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long acc = 0;
+#pragma unroll
+    for (int w = 0; w < kGenThreads / 32; ++w) acc += s_warp[w];
+    a.tagg[tile] = acc;
+  }
+}
+
+// One CTA: exclusive prefixes of the tile totals (count << 32 | edges) into
+// tincl, the totals into the control block and the pointer sentinel
+// (subgraph_generator.cu:160).
+constexpr int kGenScanThreads = 1024;
+__global__ void __launch_bounds__(kGenScanThreads) k_generate_scan(GenArgs a) {
+  __shared__ unsigned long long s_warp[kGenScanThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t per = (a.num_tiles + kGenScanThreads - 1) / kGenScanThreads;
+  const uint32_t lo = min(a.num_tiles, tid * per), hi = min(a.num_tiles, lo + per);
+  unsigned long long sum = 0;
+  for (uint32_t t = lo; t < hi; ++t) sum += a.tagg[t];
+  unsigned long long incl = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    unsigned long long acc = 0;
-    if (lane == 0) {
+    unsigned long long w = s_warp[lane];
+    unsigned long long wi = w;
 #pragma unroll
-      for (int w = 0; w < kGenThreads / 32; ++w) {
-        unsigned long long x = s_warp[w];
-        s_warp[w] = acc;
-        acc += x;
-      }
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= d) wi += y;
     }
-    acc = __shfl_sync(0xffffffffu, acc, 0);
-    const unsigned long long excl = lookback_warp(tile, acc, a.tflag, a.tagg, a.tincl, a.epoch, a.ctl, lane);
-    if (lane == 0) {
-      s_prefix = excl;
-      if (tile == a.num_tiles - 1) {
-        const unsigned long long tot = excl + acc;
-        const uint32_t c = (uint32_t)(tot >> 32);
-        a.ctl->num_active = c;
-        a.ctl->num_active_edges = tot & 0xffffffffull;
-        a.ptr[c] = (uint32_t)(tot & 0xffffffffull);  // sentinel (subgraph_generator.cu:160)
-      }
+    s_warp[lane] = wi - w;
+    if (lane == 31) {
+      const uint32_t c = (uint32_t)(wi >> 32);
+      a.ctl->num_active = c;
+      a.ctl->num_active_edges = wi & 0xffffffffull;
+      a.ptr[c] = (uint32_t)(wi & 0xffffffffull);
     }
   }
   __syncthreads();
-  if (keepmask) {
-    const unsigned long long run = s_prefix + s_warp[warp] +
-                                   (((unsigned long long)(incl_c - cnt) << 32) | (incl_e - edges));
+  unsigned long long run = s_warp[warp] + incl - sum;
+  for (uint32_t t = lo; t < hi; ++t) {
+    const unsigned long long x = a.tagg[t];
+    a.tincl[t] = run;
+    run += x;
+  }
+}
+
+__global__ void __launch_bounds__(kGenThreads) k_generate_write(GenArgs a) {
+  __shared__ unsigned long long s_warp[kGenThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t v0 = tile * kGenTile + warp * (32 * kGenRounds) + lane * kGenVPerLane;
+  const bool full = v0 + kGenVPerLane <= a.n;
+  GenLane L;
+  if (v0 < a.n) gen_lane(a, v0, full, L);
+  if (L.clearmask) {
+    uint32_t cw[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      cw[q] = 0;
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if ((L.clearmask >> (4 * q + b)) & 1u) cw[q] |= 0xffu << (8 * b);
+    }
+    if (full) {
+      *reinterpret_cast<uint4 *>(a.l1 + v0) =
+          make_uint4(L.l1w[0] & ~cw[0], L.l1w[1] & ~cw[1], L.l1w[2] & ~cw[2], L.l1w[3] & ~cw[3]);
+      *reinterpret_cast<uint4 *>(a.l2 + v0) =
+          make_uint4(L.l2w[0] & ~cw[0], L.l2w[1] & ~cw[1], L.l2w[2] & ~cw[2], L.l2w[3] & ~cw[3]);
+    } else {
+      for (uint32_t k = 0; k < kGenVPerLane; ++k)
+        if ((L.clearmask >> k) & 1u) { a.l1[v0 + k] = 0; a.l2[v0 + k] = 0; }
+    }
+  }
+  const uint32_t incl_c = warp_incl_scan(L.cnt, lane);
+  const uint32_t incl_e = warp_incl_scan(L.edges, lane);
+  if (lane == 31) s_warp[warp] = ((unsigned long long)incl_c << 32) | incl_e;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long acc = a.tincl[tile];
+#pragma unroll
+    for (int w = 0; w < kGenThreads / 32; ++w) {
+      const unsigned long long x = s_warp[w];
+      s_warp[w] = acc;
+      acc += x;
+    }
+  }
+  __syncthreads();
+  if (L.keepmask) {
+    const unsigned long long run = s_warp[warp] + (((unsigned long long)(incl_c - L.cnt) << 32) | (incl_e - L.edges));
     uint32_t pos = (uint32_t)(run >> 32), ep = (uint32_t)(run & 0xffffffffull);
 #pragma unroll
     for (uint32_t k = 0; k < kGenVPerLane; ++k) {
-      if ((keepmask >> k) & 1u) {
+      if ((L.keepmask >> k) & 1u) {
         a.queue[pos] = v0 + k;
         a.ptr[pos] = ep;
         ++pos;
-        ep += o[k + 1] - o[k];
+        ep += L.o[k + 1] - L.o[k];
       }
-    }
-  }
-  if (tid == 0) {
-    __threadfence();
-    if (atomicAdd(&a.ctl->tile_done, 1u) == a.num_tiles - 1) {
-      a.ctl->tile_ticket = 0;
-      a.ctl->tile_done = 0;
     }
   }
 }
