@@ -97,6 +97,32 @@ def test_generate_matches_reference_compaction(gpu, orc, g12u):
     assert ptr[-1] == p[-1]
 
 
+def test_generate_many_tiles_ragged(gpu, orc):
+    """Over a thousand 4096-vertex tiles (each thread of the tile scan takes
+    several) and a partial last tile: the compaction of an all-active start
+    equals the reference's, and BFS/SSSP equal the oracle under a budget that
+    forces many partitions."""
+    g = gpu.Graph.er(5_000_011, 20_000_000, seed=17, weighted=True, wmax=64)
+    eng = gpu.Engine(g, budget_bytes=18 * g.n + 4 * 1024 * 1024 + (1 << 22) * 4)
+    eng.state_init("cc", "sync")
+    nodes, ptr = eng.read_active()
+    deg = g.out_degree()
+    q, p = orc.generate(np.zeros(g.n, np.uint8), np.ones(g.n, np.uint8), deg)
+    keep = deg[q] > 0
+    assert np.array_equal(nodes, q[keep])
+    assert np.array_equal(ptr[:-1], p[:-1][keep])
+    assert ptr[-1] == p[-1]
+    src = int(g.pick_sources(1, seed=4)[0])
+    for algo in ("bfs", "sssp"):
+        e = g.edges if algo == "sssp" else np.ascontiguousarray(g.edges[:, 0])
+        ref = orc.run(algo, g.node_pointer, e, src, parallel=True)
+        for mode in MODES:
+            vals, st = eng.run(algo, mode, src)
+            assert np.array_equal(vals, ref), (algo, mode)
+            assert st["partitions"] > st["global_iterations"]
+    eng.close()
+
+
 def test_step_api_loop(gpu, orc, g12w):
     """The reference's app loop written against the step API."""
     g = g12w
