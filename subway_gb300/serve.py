@@ -9,6 +9,14 @@ fit in what the graphs admitted before it left.
 
     python -m subway_gb300.serve --scales 22 24 26 --queries 4096 --rate 2000
 prints one JSON line with p50/p99 latency and queries per second.
+
+Replicas: launched under torchrun (one process per GPU, RANK / WORLD_SIZE /
+LOCAL_RANK from the environment), every rank draws the same seeded query
+stream, serves the queries whose index is congruent to its rank on its own
+GPU with its own copy of the graphs, and rank 0 merges the latencies into one
+line; QPS is all queries over the span from the first arrival to the last
+answer on any rank.  The ranks meet only for a barrier before the clocks
+start and for the final gather.
 """
 from __future__ import annotations
 
@@ -40,11 +48,24 @@ def admit(graphs, lanes, budget_bytes, device=0, chunk_edges=0):
     return admitted, rejected
 
 
-def serve(batches, algo="bfs", queries=4096, rate=2000.0, seed=5, lanes=64):
+def make_stream(graph_sizes, queries=4096, rate=2000.0, seed=5):
+    """Seeded Poisson arrivals (s), target graph and source vertex per query."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, queries))
-    target = rng.integers(0, len(batches), queries)
-    sources = np.array([rng.integers(0, batches[t].graph.n) for t in target], np.uint32)
+    target = rng.integers(0, len(graph_sizes), queries)
+    sources = np.array([rng.integers(0, graph_sizes[t]) for t in target], np.uint32)
+    return arrivals, target, sources
+
+
+def shard(stream, world=1, rank=0):
+    """The queries of one replica: every world-th query, starting at rank."""
+    return tuple(x[rank::world] for x in stream)
+
+
+def serve_stream(batches, arrivals, target, sources, algo="bfs", lanes=64):
+    """Serves one stream in real time; returns answer times (s from the
+    start of the clock) and the batch sizes."""
+    queries = len(arrivals)
     done = np.zeros(queries)
     pending = [[] for _ in batches]  # query ids per graph, in arrival order
     sizes = []
@@ -69,12 +90,40 @@ def serve(batches, algo="bfs", queries=4096, rate=2000.0, seed=5, lanes=64):
         done[ids] = t
         served += len(ids)
         sizes.append(len(ids))
+    return done, sizes
+
+
+def summarize(arrivals, done, sizes, rate, algo):
     lat_ms = (done - arrivals) * 1e3
-    span = done.max() - arrivals[0]
-    return {"queries": queries, "rate_per_s": rate, "algo": algo, "p50_ms": float(np.percentile(lat_ms, 50)),
-            "p99_ms": float(np.percentile(lat_ms, 99)), "mean_ms": float(lat_ms.mean()),
-            "qps": queries / span, "batches": len(sizes), "mean_batch": float(np.mean(sizes)),
-            "max_batch": int(max(sizes))}
+    span = done.max() - arrivals.min()
+    return {"queries": int(len(arrivals)), "rate_per_s": rate, "algo": algo,
+            "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+            "mean_ms": float(lat_ms.mean()), "qps": len(arrivals) / span, "batches": len(sizes),
+            "mean_batch": float(np.mean(sizes)), "max_batch": int(max(sizes))}
+
+
+def serve(batches, algo="bfs", queries=4096, rate=2000.0, seed=5, lanes=64):
+    arrivals, target, sources = make_stream([b.graph.n for b in batches], queries, rate, seed)
+    done, sizes = serve_stream(batches, arrivals, target, sources, algo, lanes)
+    return summarize(arrivals, done, sizes, rate, algo)
+
+
+def serve_replicas(batches, pg, algo="bfs", queries=4096, rate=2000.0, seed=5, lanes=64):
+    """One replica's share of the stream; rank 0 returns the merged summary,
+    the other ranks None.  pg: torch.distributed, initialised."""
+    world, rank = pg.get_world_size(), pg.get_rank()
+    arrivals, target, sources = shard(make_stream([b.graph.n for b in batches], queries, rate, seed), world, rank)
+    pg.barrier()
+    done, sizes = serve_stream(batches, arrivals, target, sources, algo, lanes)
+    parts = [None] * world
+    pg.all_gather_object(parts, (arrivals, done, sizes))
+    if rank != 0:
+        return None
+    res = summarize(np.concatenate([p[0] for p in parts]), np.concatenate([p[1] for p in parts]),
+                    [x for p in parts for x in p[2]], rate, algo)
+    res["replicas"] = world
+    res["queries_per_replica"] = [int(len(p[0])) for p in parts]
+    return res
 
 
 def main():
@@ -88,6 +137,13 @@ def main():
     ap.add_argument("--chunk-edges", type=int, default=0)
     ap.add_argument("--autotune", action="store_true", help="pick each graph's edges per work item by timing")
     a = ap.parse_args()
+    import os
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as pg
+        pg.init_process_group("gloo")
     t = time.time()
     graphs = [N.Graph.rmat(s, 16, seed=5000 + s, weighted=True, wmax=64) for s in a.scales]
     t_gen = time.time() - t
@@ -95,19 +151,27 @@ def main():
     tuned = None
     if a.autotune:
         from .autotune import tune_batch
-        tuned = [tune_batch(g, a.algo, a.lanes) for g in graphs]
+        tuned = [tune_batch(g, a.algo, a.lanes, device=device) for g in graphs]
         chunks = [best for best, _ in tuned]
-    admitted, rejected = admit(graphs, a.lanes, int(a.budget), chunk_edges=chunks)
+    admitted, rejected = admit(graphs, a.lanes, int(a.budget), device=device, chunk_edges=chunks)
     # warm the graphs up once
     for b in admitted:
         b.run(a.algo, np.zeros(1, np.uint32))
-    res = serve(admitted, a.algo, a.queries, a.rate, lanes=a.lanes)
+    if pg:
+        res = serve_replicas(admitted, pg, a.algo, a.queries, a.rate, lanes=a.lanes)
+        if res is None:
+            pg.destroy_process_group()
+            return
+    else:
+        res = serve(admitted, a.algo, a.queries, a.rate, lanes=a.lanes)
     if tuned:
         res["autotune"] = [{"scale": s, "chunk_edges": best, "trials_ms": [(c, round(ms, 2)) for c, ms in trials]}
                            for s, (best, trials) in zip(a.scales, tuned)]
     res.update({"scales_admitted": [s for s, g in zip(a.scales, graphs) if g not in rejected],
                 "device_bytes": sum(b.device_bytes() for b in admitted), "generate_s": round(t_gen, 1)})
     print(json.dumps(res))
+    if pg:
+        pg.destroy_process_group()
 
 
 if __name__ == "__main__":
