@@ -355,11 +355,13 @@ def probe_link(N, dev):
     return h.value, d.value
 
 
-# DRAM bytes (read + write) per algorithmic byte, from one ncu capture of
-# each kernel on a small case (profiles/k_gather_v_rmat21.md, launch 3;
-# profiles/k_relax_tile_rmat21.md; profiles/k_generate_rmat21.md); a full-size
-# launch's traffic is this ratio times its algorithmic bytes.
-DRAM_PER_ALGO_BYTE = {"gather": 1.21}
+# DRAM bytes (read + write) per algorithmic byte, from ncu captures on small
+# cases: gather from profiles/k_gather_v_rmat21.md (launch 3); relax and
+# generate from every launch of one RMAT-22 SSSP-async run under a 300 MB
+# budget (profiles/dram_traffic_rmat22_sssp_async.md; ncu empties the caches
+# before each launch, so these are cold-cache figures).  A full-size launch's
+# traffic is this ratio times its algorithmic bytes.
+DRAM_PER_ALGO_BYTE = {"gather": 1.21, "relax": 0.93, "generate": 2.36}
 
 
 def traffic_per_launch(name, bytes_per_launch):
