@@ -1627,8 +1627,8 @@ int sgw_run(sgw_engine *e, const sgw_run_params *p, void *out_values, sgw_run_st
 }  // extern "C"
 
 // ---- allocation-free compaction ---------------------------------------------
-// sgw_generate_noalloc runs the engine's generate kernel (k_generate) on
-// caller-owned device arrays, with the scan's tile state and counters in the
+// sgw_generate_noalloc runs the single-pass generate kernel (k_generate, one
+// launch, decoupled look-back) on caller-owned device arrays, with the scan's tile state and counters in the
 // file-scope array below instead of an engine arena.  Nothing here allocates.
 //
 // Limit: SGW_NOALLOC_MAX_VERTICES vertices = 16384 scan tiles of 4096.
