@@ -69,6 +69,17 @@ const char *sgw_last_error(void);
  * outDegree[n-2] unset, shared/graph.cu:179-181). */
 int sgw_graph_load(const char *path, sgw_graph **out);
 
+/* Maps a .bcsr/.bwcsr file instead of reading it (shared/graph.cu:41-51
+ * freads the whole file into pinned memory): the edge records stay in the
+ * read-only file mapping, shared with the page cache, and only the n node
+ * pointers are copied (plus the sentinel node_pointer[n] = m, which the file
+ * does not hold).  The file is validated like sgw_graph_load (size, monotone
+ * pointers, endpoints < n), which reads every record once.  The mapping is
+ * released by sgw_graph_free; the file must not be truncated meanwhile.
+ * A .bwcsr file with an odd vertex count is read as by sgw_graph_load
+ * instead, since its 8-byte records would not be 8-byte aligned. */
+int sgw_graph_map(const char *path, sgw_graph **out);
+
 /* Wraps a caller-owned host CSR without copying it.  node_pointer has n+1
  * entries (node_pointer[n] == m); edges holds m records of 4 B (weighted=0)
  * or 8 B (weighted=1).  The arrays must outlive the graph object and every

@@ -181,7 +181,12 @@ int main(int argc, char **argv) {
   double t0 = now_ms();
   printf("Reading the input graph from the following file:\n>> %s\n", a.input.c_str());
   sgw_graph *g = nullptr;
-  int st = sgw_graph_load(a.input.c_str(), &g);
+  // binary files are mapped in place (the edges stay in the page cache),
+  // text files parsed
+  const size_t dot = a.input.find_last_of('.');
+  const std::string ext = dot == std::string::npos ? "" : a.input.substr(dot + 1);
+  int st = (ext == "bcsr" || ext == "bwcsr") ? sgw_graph_map(a.input.c_str(), &g)
+                                             : sgw_graph_load(a.input.c_str(), &g);
   if (st != SGW_OK) die(st, "ReadGraph");
   uint32_t n = 0, m = 0;
   int weighted = 0;

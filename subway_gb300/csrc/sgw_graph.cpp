@@ -725,11 +725,86 @@ int sgw_graph_save(const sgw_graph *g, const char *path) {
 
 void sgw_graph_free(sgw_graph *g) {
   if (!g) return;
-  if (g->owns) {
+  if (g->map_base) {
+    host_free(g->node_pointer);
+    munmap(g->map_base, g->map_len);
+  } else if (g->owns) {
     host_free(g->node_pointer);
     host_free(g->edges);
   }
   delete g;
+}
+
+int sgw_graph_map(const char *path, sgw_graph **out) {
+  clear_error();
+  if (!path || !out) return fail(SGW_EINVAL, "null argument");
+  *out = nullptr;
+  const std::string ext = extension_of(path);
+  if (ext != "bcsr" && ext != "bwcsr")
+    return fail(SGW_EFORMAT, "only .bcsr/.bwcsr files can be mapped: '%s'", path);
+  const int weighted = ext == "bwcsr";
+  int fd = open(path, O_RDONLY);
+  if (fd < 0) return fail(SGW_EIO, "cannot open %s", path);
+  struct stat sb;
+  uint32_t hdr[2];
+  if (fstat(fd, &sb) != 0 || pread(fd, hdr, sizeof(hdr), 0) != (ssize_t)sizeof(hdr)) {
+    close(fd);
+    return fail(SGW_EFORMAT, "%s: truncated header", path);
+  }
+  const uint32_t n = hdr[0], m = hdr[1], esz = weighted ? 8 : 4;
+  const long long want = 8LL + 4LL * n + (long long)m * esz;
+  if (n == 0) { close(fd); return fail(SGW_EFORMAT, "%s: zero vertices", path); }
+  if ((long long)sb.st_size != want) {
+    close(fd);
+    return fail(SGW_EFORMAT, "%s: size %lld, expected %lld for n=%u m=%u", path,
+                (long long)sb.st_size, want, n, m);
+  }
+  if (weighted && (n & 1u)) {  // 8-byte records would start 4 bytes off an 8-byte boundary
+    close(fd);
+    return load_binary(path, weighted, out);
+  }
+  void *base = mmap(nullptr, (size_t)want, PROT_READ, MAP_SHARED, fd, 0);
+  close(fd);
+  if (base == MAP_FAILED) return fail(SGW_EIO, "cannot map %s", path);
+  madvise(base, (size_t)want, MADV_WILLNEED);
+  uint32_t *np = (uint32_t *)host_alloc(sizeof(uint32_t) * (size_t(n) + 1), nullptr);
+  sgw_graph *g = np ? new (std::nothrow) sgw_graph() : nullptr;
+  if (!g) {
+    host_free(np);
+    munmap(base, (size_t)want);
+    return fail(SGW_ENOMEM, "graph arrays (n=%u)", n);
+  }
+  const uint32_t *fnp = (const uint32_t *)((const char *)base + 8);
+#pragma omp parallel for
+  for (int64_t v = 0; v < (int64_t)n; ++v) np[v] = fnp[v];
+  np[n] = m;
+  g->n = n;
+  g->m = m;
+  g->weighted = weighted;
+  g->esz = esz;
+  g->owns = false;
+  g->node_pointer = np;
+  g->edges = (char *)base + 8 + 4 * size_t(n);
+  g->map_base = base;
+  g->map_len = (size_t)want;
+  int bad = 0;
+#pragma omp parallel for reduction(| : bad)
+  for (int64_t v = 0; v < (int64_t)n; ++v)
+    if (np[v] > np[v + 1]) bad |= 1;
+  if (!bad) {
+    const uint32_t *ed = (const uint32_t *)g->edges;
+    const size_t stride = esz / 4;
+#pragma omp parallel for reduction(| : bad)
+    for (int64_t i = 0; i < (int64_t)m; ++i)
+      if (ed[size_t(i) * stride] >= n) bad |= 2;
+  }
+  if (bad) {
+    sgw_graph_free(g);
+    return fail(SGW_EFORMAT, "%s: %s", path,
+                (bad & 1) ? "node pointers not monotone" : "edge endpoint out of range");
+  }
+  *out = g;
+  return SGW_OK;
 }
 
 int sgw_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b,

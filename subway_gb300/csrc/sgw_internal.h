@@ -16,6 +16,8 @@ struct sgw_graph {
   void *edges = nullptr;          // m * esz bytes, page aligned when owned
   bool owns = false;              // arrays allocated (and freed) by the library
   size_t edges_bytes_alloc = 0;   // rounded allocation size of edges
+  void *map_base = nullptr;       // sgw_graph_map: the file mapping holding edges
+  size_t map_len = 0;
 };
 
 namespace sgw {

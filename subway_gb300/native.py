@@ -69,6 +69,7 @@ _PROTOS = {
     "sgw_strerror": (C.c_char_p, [C.c_int]),
     "sgw_last_error": (C.c_char_p, []),
     "sgw_graph_load": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
+    "sgw_graph_map": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "sgw_graph_from_csr": (C.c_int, [C.c_uint32, C.c_uint32, _P, _P, C.c_int, C.POINTER(_P)]),
     "sgw_graph_info": (C.c_int, [_P, _u32p, _u32p, C.POINTER(C.c_int)]),
     "sgw_graph_node_pointer": (_P, [_P]),
@@ -212,6 +213,13 @@ class Graph:
     def load(cls, path):
         h = _P()
         check(lib().sgw_graph_load(str(path).encode(), C.byref(h)), f"sgw_graph_load({path})")
+        return cls(h.value)
+
+    @classmethod
+    def map(cls, path):
+        """A .bcsr/.bwcsr file mapped in place: edges stay in the page cache."""
+        h = _P()
+        check(lib().sgw_graph_map(str(path).encode(), C.byref(h)), f"sgw_graph_map({path})")
         return cls(h.value)
 
     @classmethod

@@ -123,6 +123,24 @@ def test_generate_many_tiles_ragged(gpu, orc):
     eng.close()
 
 
+def test_engine_on_mapped_graph(gpu, orc, tmp_path):
+    """A .bwcsr / .bcsr file mapped in place (edges in the page cache) runs
+    like a loaded one."""
+    for weighted in (True, False):
+        g = _graph(gpu, 14, weighted, seed=23)
+        p = tmp_path / ("g.bwcsr" if weighted else "g.bcsr")
+        g.save(p)
+        h = gpu.Graph.map(p)
+        eng = gpu.Engine(h, budget_bytes=18 * h.n + 96 * 1024 + 20000 * 8)
+        src = int(g.pick_sources(1, seed=2)[0])
+        for algo in ("bfs", "sssp") if weighted else ("bfs", "cc"):
+            for mode in MODES:
+                vals, _ = eng.run(algo, mode, src)
+                assert np.array_equal(vals, _oracle(orc, g, algo, src)), (weighted, algo, mode)
+        eng.close()
+        h.close()
+
+
 def test_step_api_loop(gpu, orc, g12w):
     """The reference's app loop written against the step API."""
     g = g12w

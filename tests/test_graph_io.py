@@ -221,3 +221,38 @@ def test_text_errors_name_the_first_bad_line(native, tmp_path):
     (tmp_path / "empty.el").write_text("# only a comment\n\n")
     with pytest.raises(native.SgwError):
         native.Graph.load(tmp_path / "empty.el")
+
+
+@pytest.mark.parametrize("ext,n_odd", [("bcsr", False), ("bwcsr", False), ("bcsr", True), ("bwcsr", True)])
+def test_mapped_binary_equals_loaded(native, tmp_path, ext, n_odd):
+    weighted = ext == "bwcsr"
+    if n_odd:
+        g = native.Graph.er(4099, 40000, seed=8, weighted=weighted)
+    else:
+        g = native.Graph.rmat(12, 8, seed=8, weighted=weighted)
+    p = tmp_path / f"g.{ext}"
+    g.save(p)
+    a = native.Graph.load(p)
+    b = native.Graph.map(p)
+    assert (b.n, b.m, b.weighted) == (a.n, a.m, a.weighted)
+    assert np.array_equal(b.node_pointer, a.node_pointer)
+    assert np.array_equal(b.edges, a.edges)
+    if weighted:
+        assert native.lib().sgw_graph_edges(b.h) % 8 == 0
+    del b  # releases the mapping
+    assert np.array_equal(native.Graph.map(p).out_degree(), g.out_degree())
+
+
+def test_mapped_binary_errors(native, tmp_path):
+    g = native.Graph.rmat(8, 4, seed=1)
+    g.save(tmp_path / "t.bcsr")
+    raw = (tmp_path / "t.bcsr").read_bytes()
+    (tmp_path / "trunc.bcsr").write_bytes(raw[:-4])
+    bad = bytearray(raw)
+    bad[-4:] = np.uint32(10**6).tobytes()
+    (tmp_path / "bad.bcsr").write_bytes(bytes(bad))
+    (tmp_path / "g.el").write_text("0 1\n")
+    for name, status in (("missing.bcsr", -2), ("trunc.bcsr", -3), ("bad.bcsr", -3), ("g.el", -3)):
+        with pytest.raises(native.SgwError) as e:
+            native.Graph.map(tmp_path / name)
+        assert e.value.status == status, name
