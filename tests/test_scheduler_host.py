@@ -42,3 +42,26 @@ def test_mispredictions_against_break_even():
     assert m["transfer_mispredicted"] == 2
     assert abs(m["prediction_mae"] - np.mean([0.2, 0.2, 0.65, 0.0])) < 1e-4
     assert scheduler.mispredictions(rec[:0])["transfer_decisions"] == 0
+
+
+def test_sched_buffers_rule():
+    """3 edge buffers when a third of the space left after the 18 B/vertex
+    state holds at least 15% of the edges at the transfer record size (4 B
+    packed or unweighted, 8 B for weights that neither pack beside the ids nor
+    fit a byte), else 2."""
+    g = N.Graph.rmat(12, 16, seed=3, weighted=True, wmax=64)  # packs: 4 B records
+    state = 18 * g.n
+    edge = int(np.ceil(0.15 * g.m)) * 4 * 3
+    assert N.sched_buffers(g, state + edge) == 3
+    assert N.sched_buffers(g, state + edge - 16) == 2
+    assert N.sched_buffers(g, state) == 2
+    assert N.sched_buffers(g, 0) == 2
+    u = N.Graph.rmat(12, 16, seed=3)
+    assert N.sched_buffers(u, 18 * u.n + int(np.ceil(0.15 * u.m)) * 12) == 3
+    # weights of 2^24 leave no room beside 12-bit ids: 8-byte records
+    e = g.edges.copy()
+    e[:, 1] = 1 << 24
+    w = N.Graph.from_csr(g.node_pointer, e, True)
+    need8 = int(np.ceil(0.15 * w.m)) * 8 * 3
+    assert N.sched_buffers(w, 18 * w.n + need8) == 3
+    assert N.sched_buffers(w, 18 * w.n + need8 // 2) == 2
