@@ -256,3 +256,41 @@ def test_mapped_binary_errors(native, tmp_path):
         with pytest.raises(native.SgwError) as e:
             native.Graph.map(tmp_path / name)
         assert e.value.status == status, name
+
+
+def test_text_reader_survives_random_bytes(native, tmp_path):
+    """Random bytes, digits and separators (including lines cut anywhere and
+    pieces of more than 1 MiB): the reader returns a graph or an error status,
+    and whatever it accepts round-trips through the binary format."""
+    rng = np.random.default_rng(99)
+    alphabet = np.frombuffer(b"0123456789 \t\r\n#%-x", np.uint8)
+    accepted = 0
+    for k in range(18):
+        size = int(rng.choice([1, 7, 100, 5000, 1_500_000]))
+        if k % 3 == 0:
+            data = rng.integers(0, 256, size, dtype=np.uint8).tobytes()
+        elif k % 3 == 1:
+            data = alphabet[rng.integers(0, len(alphabet), size)].tobytes()
+        else:  # whole "src dst w" lines with random blanks, comments and CRs
+            lines = []
+            for _ in range(size // 12 + 1):
+                a, b, w = (int(x) for x in rng.integers(0, 5000, 3))
+                sep = str(rng.choice([" ", "\t", "  "]))
+                lines.append(f"{a}{sep}{b}{sep}{w}" + str(rng.choice(["", "\r", " #x"])))
+                if rng.random() < 0.05:
+                    lines.append(str(rng.choice(["", "# c", "%"])))
+            data = "\n".join(lines).encode()
+        for ext in ("el", "wel"):
+            p = tmp_path / f"f{k}.{ext}"
+            p.write_bytes(data)
+            try:
+                g = native.Graph.load(p)
+            except native.SgwError as e:
+                assert e.status in (-3, -4, -9)
+                continue
+            accepted += 1
+            q = tmp_path / f"f{k}.{'bwcsr' if ext == 'wel' else 'bcsr'}"
+            g.save(q)
+            h = native.Graph.load(q)
+            assert np.array_equal(h.node_pointer, g.node_pointer) and np.array_equal(h.edges, g.edges)
+    assert accepted > 0
