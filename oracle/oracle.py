@@ -22,7 +22,7 @@ def lib():
     if _lib is None:
         path = build_oracle() if not OUT.exists() else OUT
         L = C.CDLL(str(path))
-        for name in ("orc_bfs", "orc_sssp", "orc_sswp", "omp_bfs", "omp_sssp", "omp_sswp"):
+        for name in ("orc_bfs", "orc_sssp", "orc_sswp", "omp_bfs", "omp_sssp", "omp_sswp", "omp_sssp_frontier"):
             getattr(L, name).argtypes = [C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, _P]
             getattr(L, name).restype = C.c_int
         for name in ("orc_cc", "omp_cc"):
@@ -37,6 +37,13 @@ def lib():
         L.orc_partition.argtypes = [_P, C.c_uint32, C.c_uint64, _P, _P, C.c_uint32]
         L.orc_partition.restype = C.c_uint32
         L.orc_num_threads.restype = C.c_int
+        L.orc_rmat_write.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                     C.c_uint64, C.c_int, C.c_uint32, C.c_char_p, C.POINTER(C.c_uint64)]
+        L.orc_rmat_write.restype = C.c_int
+        L.orc_pick_sources.argtypes = [C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, C.c_uint64, _P]
+        L.orc_pick_sources.restype = C.c_int
+        L.omp_reach_multi.argtypes = [C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, _P, _P]
+        L.omp_reach_multi.restype = C.c_int
         _lib = L
     return _lib
 
@@ -104,3 +111,62 @@ def partition(ptr, max_partition_size):
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+def rmat_write(path, scale, edge_factor=16, seed=1, weighted=False, wmax=64, a=0.57, b=0.19, c=0.19) -> int:
+    """Writes the seeded R-MAT graph as a .bcsr/.bwcsr file; returns its edge count."""
+    m = C.c_uint64()
+    st = lib().orc_rmat_write(scale, edge_factor, a, b, c, seed, int(weighted), wmax, str(path).encode(),
+                              C.byref(m))
+    if st != 0:
+        raise RuntimeError(f"oracle R-MAT writer failed ({st})")
+    return m.value
+
+
+def read_csr(path):
+    """(node_pointer[n+1], edges) of a .bcsr/.bwcsr file; edges map the file in place."""
+    hdr = np.fromfile(path, dtype=np.uint32, count=2)
+    n, m = int(hdr[0]), int(hdr[1])
+    npa = np.empty(n + 1, np.uint32)
+    npa[:n] = np.memmap(path, dtype=np.uint32, mode="r", offset=8, shape=(n,))
+    npa[n] = m
+    weighted = str(path).endswith(".bwcsr")
+    shape = (m, 2) if weighted else (m,)
+    edges = np.memmap(path, dtype=np.uint32, mode="r", offset=8 + 4 * n, shape=shape) if m else \
+        np.zeros(shape, np.uint32)
+    return npa, edges
+
+
+def pick_sources(node_pointer, edges, count, seed=1) -> np.ndarray:
+    """count sources among the out-degree > 0 vertices of the largest WCC."""
+    npa, eda, stride = _csr(node_pointer, edges)
+    out = np.empty(count, np.uint32)
+    if lib().orc_pick_sources(len(npa) - 1, npa.ctypes.data, eda.ctypes.data, stride, count, seed,
+                              out.ctypes.data) != 0:
+        raise RuntimeError("oracle source picker failed")
+    return out
+
+
+def reached_edges(node_pointer, edges, sources) -> np.ndarray:
+    """m_reached (edges whose source is reachable) of each source, <= 64 per call."""
+    npa, eda, stride = _csr(node_pointer, edges)
+    src = np.ascontiguousarray(sources, dtype=np.uint32)
+    out = np.zeros(len(src), np.uint64)
+    for k in range(0, len(src), 64):
+        part = np.ascontiguousarray(src[k:k + 64])
+        res = np.zeros(len(part), np.uint64)
+        if lib().omp_reach_multi(len(npa) - 1, npa.ctypes.data, eda.ctypes.data, stride, len(part),
+                                 part.ctypes.data, res.ctypes.data) != 0:
+            raise RuntimeError("oracle reachability failed")
+        out[k:k + 64] = res
+    return out
+
+
+def sssp_frontier(node_pointer, edges, source) -> np.ndarray:
+    """SSSP by unbucketed frontier rounds (a second exact method)."""
+    npa, eda, stride = _csr(node_pointer, edges)
+    out = np.empty(len(npa) - 1, np.uint32)
+    if lib().omp_sssp_frontier(len(npa) - 1, npa.ctypes.data, eda.ctypes.data, stride, int(source),
+                               out.ctypes.data) != 0:
+        raise RuntimeError("oracle sssp failed")
+    return out

@@ -32,6 +32,7 @@
 #include <math.h>
 #include <omp.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -378,9 +379,185 @@ static int omp_frontier(int algo, uint32_t n, const uint32_t *np, const uint32_t
 int omp_bfs(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
   return omp_frontier(0, n, np, ed, stride, src, out, 0);
 }
+/* Appends v to a shared array through a thread-local block of 1024. */
+typedef struct { uint32_t buf[1024]; int n; } tl_buf;
+static inline void tl_push(tl_buf *b, uint32_t v, uint32_t *out, size_t *cnt) {
+  b->buf[b->n++] = v;
+  if (b->n == 1024) {
+    size_t at = __atomic_fetch_add(cnt, (size_t)b->n, __ATOMIC_RELAXED);
+    memcpy(out + at, b->buf, sizeof(uint32_t) * b->n);
+    b->n = 0;
+  }
+}
+static inline void tl_flush(tl_buf *b, uint32_t *out, size_t *cnt) {
+  if (b->n) {
+    size_t at = __atomic_fetch_add(cnt, (size_t)b->n, __ATOMIC_RELAXED);
+    memcpy(out + at, b->buf, sizeof(uint32_t) * b->n);
+    b->n = 0;
+  }
+}
+
+/* Delta-stepping SSSP (Meyer and Sanders, J. Algorithms 2003), in the
+ * label-correcting form: bucket k holds the vertices whose distance lies in
+ * [k*delta, (k+1)*delta).  Rounds relax the out-edges of the current bucket's
+ * changed vertices until the bucket is empty; an improvement beyond the
+ * bucket parks the vertex in a pending list, from which the next non-empty
+ * bucket is taken.  Every vertex whose distance changes has its out-edges
+ * relaxed afterwards, so the result is the exact fixpoint (the same labels as
+ * orc_sssp); the buckets only cut repeated relaxations. */
+static int omp_delta_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t src,
+                          uint32_t delta, uint32_t *val) {
+  uint32_t *front = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t *next = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t *pend = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
+  uint8_t *inq = (uint8_t *)calloc(n, 1);   /* queued for the next round */
+  uint8_t *inp = (uint8_t *)calloc(n, 1);   /* in the pending list */
+  if (!front || !next || !pend || !inq || !inp) {
+    free(front); free(next); free(pend); free(inq); free(inp);
+    return -1;
+  }
+#pragma omp parallel for
+  for (int64_t v = 0; v < (int64_t)n; ++v) val[v] = ORC_INF;
+  val[src] = 0;
+  front[0] = src;
+  size_t nf = 1, np_ = 0;
+  uint64_t bucket = 0;
+  for (;;) {
+    const uint64_t hi = (bucket + 1) * (uint64_t)delta;  /* bucket's end */
+    while (nf) {
+      size_t nn = 0;
+#pragma omp parallel
+      {
+        tl_buf bn, bp;
+        bn.n = bp.n = 0;
+#pragma omp for schedule(dynamic, 64) nowait
+        for (int64_t k = 0; k < (int64_t)nf; ++k) {
+          const uint32_t u = front[k];
+          const uint32_t du = __atomic_load_n(&val[u], __ATOMIC_RELAXED);
+          for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+            const uint32_t v = ed[2 * (size_t)i];
+            const uint32_t c = du + ed[2 * (size_t)i + 1];
+            if (!cas_min(&val[v], c)) continue;
+            if (c < hi) {
+              if (!__atomic_exchange_n(&inq[v], 1, __ATOMIC_RELAXED)) tl_push(&bn, v, next, &nn);
+            } else if (!__atomic_exchange_n(&inp[v], 1, __ATOMIC_RELAXED)) {
+              tl_push(&bp, v, pend, &np_);
+            }
+          }
+        }
+        tl_flush(&bn, next, &nn);
+        tl_flush(&bp, pend, &np_);
+      }
+#pragma omp parallel for
+      for (int64_t k = 0; k < (int64_t)nn; ++k) inq[next[k]] = 0;
+      uint32_t *t = front; front = next; next = t;
+      nf = nn;
+    }
+    /* next bucket: the smallest among pending vertices still beyond this
+     * one (the others were improved into a bucket already relaxed) */
+    uint64_t best = UINT64_MAX;
+#pragma omp parallel for reduction(min : best)
+    for (int64_t k = 0; k < (int64_t)np_; ++k) {
+      const uint32_t d = val[pend[k]];
+      if ((uint64_t)d >= hi && (uint64_t)d / delta < best) best = (uint64_t)d / delta;
+    }
+    if (best == UINT64_MAX) break;
+    bucket = best;
+    const uint64_t lo2 = bucket * (uint64_t)delta, hi2 = lo2 + delta;
+    size_t keep = 0;
+    nf = 0;
+    for (size_t k = 0; k < np_; ++k) {  /* serial: stable and simple */
+      const uint32_t v = pend[k];
+      const uint32_t d = val[v];
+      if ((uint64_t)d >= hi2) {
+        pend[keep++] = v;
+      } else {
+        inp[v] = 0;
+        if ((uint64_t)d >= lo2) front[nf++] = v;
+      }
+    }
+    np_ = keep;
+  }
+  free(front); free(next); free(pend); free(inq); free(inp);
+  return 0;
+}
+
 int omp_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
   if (stride != 2) return -2;
+  return omp_delta_sssp(n, np, ed, src, 32, out);
+}
+
+/* Frontier form of omp_sssp (Bellman-Ford rounds without buckets), kept as a
+ * second exact method for the tests. */
+int omp_sssp_frontier(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t src,
+                      uint32_t *out) {
+  if (stride != 2) return -2;
   return omp_frontier(1, n, np, ed, stride, src, out, 0);
+}
+
+/* Edges reachable from each of nsrc <= 64 sources (the sum of the out-degrees
+ * of the vertices a source reaches, Graph500's m_reached for BFS, SSSP and
+ * SSWP), by one bit-parallel search: every vertex carries a 64-bit mask of the
+ * sources that reach it, and a vertex whose mask gains bits pushes them along
+ * its out-edges in the next round. */
+int omp_reach_multi(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t nsrc,
+                    const uint32_t *src, uint64_t *reached) {
+  if (nsrc == 0 || nsrc > 64) return -2;
+  uint64_t *mask = (uint64_t *)calloc(n, sizeof(uint64_t));
+  uint32_t *front = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t *next = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
+  uint8_t *inq = (uint8_t *)calloc(n, 1);
+  if (!mask || !front || !next || !inq) { free(mask); free(front); free(next); free(inq); return -1; }
+  size_t nf = 0;
+  for (uint32_t k = 0; k < nsrc; ++k) {
+    if (!mask[src[k]]) front[nf++] = src[k];
+    mask[src[k]] |= 1ULL << k;
+  }
+  while (nf) {
+    size_t nn = 0;
+#pragma omp parallel
+    {
+      tl_buf b;
+      b.n = 0;
+#pragma omp for schedule(dynamic, 64) nowait
+      for (int64_t k = 0; k < (int64_t)nf; ++k) {
+        const uint32_t u = front[k];
+        const uint64_t mu = __atomic_load_n(&mask[u], __ATOMIC_RELAXED);
+        for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+          const uint32_t v = ed[(size_t)i * stride];
+          const uint64_t mv = __atomic_load_n(&mask[v], __ATOMIC_RELAXED);
+          if ((mu & ~mv) == 0) continue;
+          const uint64_t old = __atomic_fetch_or(&mask[v], mu, __ATOMIC_RELAXED);
+          if ((mu & ~old) && !__atomic_exchange_n(&inq[v], 1, __ATOMIC_RELAXED)) tl_push(&b, v, next, &nn);
+        }
+      }
+      tl_flush(&b, next, &nn);
+    }
+#pragma omp parallel for
+    for (int64_t k = 0; k < (int64_t)nn; ++k) inq[next[k]] = 0;
+    uint32_t *t = front; front = next; next = t;
+    nf = nn;
+  }
+  for (uint32_t k = 0; k < nsrc; ++k) reached[k] = 0;
+#pragma omp parallel
+  {
+    uint64_t loc[64] = {0};
+#pragma omp for schedule(static)
+    for (int64_t v = 0; v < (int64_t)n; ++v) {
+      uint64_t m = mask[v];
+      const uint64_t deg = np[v + 1] - np[v];
+      while (m) {
+        loc[__builtin_ctzll(m)] += deg;
+        m &= m - 1;
+      }
+    }
+    for (uint32_t k = 0; k < nsrc; ++k) {
+#pragma omp atomic
+      reached[k] += loc[k];
+    }
+  }
+  free(mask); free(front); free(next); free(inq);
+  return 0;
 }
 int omp_sswp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
   if (stride != 2) return -2;
@@ -433,3 +610,227 @@ int omp_pr(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, 
 }
 
 int orc_num_threads(void) { return omp_get_max_threads(); }
+
+/* ------------------------------------------------------------------------ */
+/* Seeded synthetic inputs, independent of the engine library               */
+/* ------------------------------------------------------------------------ */
+/* The benchmark's reference arm must not load the engine library, so the
+ * R-MAT graph and the source choice are restated here.  Both follow the
+ * published algorithms the engine's generator documents (include/
+ * sgw_graphgen.h): R-MAT (Chakrabarti, Zhan and Faloutsos, SDM 2004) drawn
+ * with SplitMix64 (Steele, Lea and Flood, OOPSLA 2014) indexed by edge number,
+ * self-loops, duplicates and vertex n-2's out-edges removed (so that the
+ * reference's loader, which never writes outDegree[n-2], shared/graph.cu:
+ * 179-181, means the same thing), rows sorted by destination, weight
+ * 1 + hash(src, dst) mod wmax; sources uniform among the out-degree > 0
+ * vertices of the largest weakly connected component.  The output file is
+ * the reference's binary CSR [n][m][nodePointer x n][edge x m]
+ * (shared/graph.cu:39-52).  tests/test_oracle.py checks the bytes and the
+ * sources against the engine library's generator. */
+
+static inline uint64_t sm_fin(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+#define SM_GAMMA 0x9e3779b97f4a7c15ULL
+
+/* The (src, dst) pair of edge e: one quadrant per level, 32 random bits per
+ * level, two levels per 64-bit draw (low half first). */
+static inline uint64_t rmat_pair(uint32_t scale, uint64_t ta, uint64_t tab, uint64_t tabc,
+                                 uint64_t key, uint64_t e) {
+  uint64_t state = key ^ sm_fin(e * SM_GAMMA + 0x2545f4914f6cdd1dULL);
+  uint64_t word = 0;
+  uint32_t s = 0, d = 0;
+  for (uint32_t l = 0; l < scale; ++l) {
+    uint64_t u;
+    if ((l & 1u) == 0) {
+      state += SM_GAMMA;
+      word = sm_fin(state);
+      u = word & 0xffffffffULL;
+    } else {
+      u = word >> 32;
+    }
+    const uint32_t qs = u >= tab, qd = (u >= ta && u < tab) || u >= tabc;
+    s = (s << 1) | qs;
+    d = (d << 1) | qd;
+  }
+  return ((uint64_t)s << 32) | d;
+}
+
+static int cmp_u64(const void *x, const void *y) {
+  const uint64_t a = *(const uint64_t *)x, b = *(const uint64_t *)y;
+  return (a > b) - (a < b);
+}
+
+/* Writes the R-MAT graph to `path` (.bwcsr when weighted, else .bcsr).
+ * Returns 0, -1 (memory), -2 (I/O), -3 (m reaches 2^32). */
+int orc_rmat_write(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                   uint64_t seed, int weighted, uint32_t wmax, const char *path,
+                   uint64_t *m_out) {
+  if (scale == 0 || scale > 31 || edge_factor == 0 || (weighted && wmax == 0)) return -4;
+  const uint32_t n = 1u << scale, drop = n - 2;
+  const uint64_t m0 = (uint64_t)edge_factor << scale;
+  const uint64_t ta = (uint64_t)(a * 4294967296.0), tab = (uint64_t)((a + b) * 4294967296.0),
+                 tabc = (uint64_t)((a + b + c) * 4294967296.0);
+  const uint64_t key = sm_fin(seed ^ 0x6a09e667f3bcc909ULL);
+  const uint64_t wkey = sm_fin(seed ^ 0xbb67ae8584caa73bULL);
+  /* buckets of sources by their top bits: count, place, sort, deduplicate */
+  const uint32_t bb = scale < 14 ? scale : 14, sh = scale - bb, B = 1u << bb;
+  const int T = omp_get_max_threads();
+  uint64_t *cnt = (uint64_t *)calloc((size_t)T * B, sizeof(uint64_t));
+  uint64_t *start = (uint64_t *)calloc((size_t)B + 1, sizeof(uint64_t));
+  uint64_t *uniq = (uint64_t *)calloc((size_t)B + 1, sizeof(uint64_t));
+  uint32_t *np = (uint32_t *)calloc((size_t)n + 1, sizeof(uint32_t));
+  if (!cnt || !start || !uniq || !np) { free(cnt); free(start); free(uniq); free(np); return -1; }
+#pragma omp parallel num_threads(T)
+  {
+    const int t = omp_get_thread_num();
+    uint64_t *h = cnt + (size_t)t * B;
+    const uint64_t lo = m0 * t / T, hi = m0 * (t + 1) / T;
+    for (uint64_t e = lo; e < hi; ++e) {
+      const uint64_t p = rmat_pair(scale, ta, tab, tabc, key, e);
+      const uint32_t s = (uint32_t)(p >> 32), d = (uint32_t)p;
+      if (s != d && s != drop) h[s >> sh]++;
+    }
+  }
+  uint64_t acc = 0;
+  for (uint32_t k = 0; k < B; ++k) {
+    start[k] = acc;
+    for (int t = 0; t < T; ++t) {
+      const uint64_t v = cnt[(size_t)t * B + k];
+      cnt[(size_t)t * B + k] = acc;
+      acc += v;
+    }
+  }
+  start[B] = acc;
+  uint64_t *pairs = (uint64_t *)malloc(sizeof(uint64_t) * (acc ? acc : 1));
+  if (!pairs) { free(cnt); free(start); free(uniq); free(np); return -1; }
+#pragma omp parallel num_threads(T)
+  {
+    const int t = omp_get_thread_num();
+    uint64_t *cur = cnt + (size_t)t * B;
+    const uint64_t lo = m0 * t / T, hi = m0 * (t + 1) / T;
+    for (uint64_t e = lo; e < hi; ++e) {
+      const uint64_t p = rmat_pair(scale, ta, tab, tabc, key, e);
+      const uint32_t s = (uint32_t)(p >> 32), d = (uint32_t)p;
+      if (s != d && s != drop) pairs[cur[s >> sh]++] = p;
+    }
+  }
+  free(cnt);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < (int64_t)B; ++k) {
+    uint64_t *p = pairs + start[k];
+    const uint64_t len = start[k + 1] - start[k];
+    qsort(p, len, sizeof(uint64_t), cmp_u64);
+    uint64_t u = 0;
+    for (uint64_t i = 0; i < len; ++i)
+      if (u == 0 || p[u - 1] != p[i]) p[u++] = p[i];
+    uniq[k] = u;
+    for (uint64_t i = 0; i < u; ++i) np[(p[i] >> 32) + 1]++;
+  }
+  uint64_t m = 0;
+  for (uint32_t k = 0; k < B; ++k) m += uniq[k];
+  if (m >= 0xffffffffULL) { free(pairs); free(start); free(uniq); free(np); return -3; }
+  for (uint32_t v = 0; v < n; ++v) np[v + 1] += np[v];
+  /* records in place, bucket by bucket: (dst, weight) in the same 8 bytes,
+   * or the 4-byte destination moved down within the bucket's own region */
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < (int64_t)B; ++k) {
+    uint64_t *p = pairs + start[k];
+    uint32_t *w32 = (uint32_t *)p;
+    for (uint64_t i = 0; i < uniq[k]; ++i) {
+      const uint32_t s = (uint32_t)(p[i] >> 32), d = (uint32_t)p[i];
+      if (weighted) {
+        const uint64_t h = sm_fin(wkey ^ sm_fin(((uint64_t)s << 32) | d) ^ 0x5851f42d4c957f2dULL);
+        w32[2 * i] = d;
+        w32[2 * i + 1] = 1u + (uint32_t)(h % wmax);
+      } else {
+        w32[i] = d;
+      }
+    }
+  }
+  int st = 0;
+  FILE *f = fopen(path, "wb");
+  if (!f) st = -2;
+  if (!st) {
+    const uint32_t hdr[2] = {n, (uint32_t)m};
+    if (fwrite(hdr, 4, 2, f) != 2 || fwrite(np, 4, n, f) != n) st = -2;
+  }
+  const size_t rec = weighted ? 8 : 4;
+  for (uint32_t k = 0; k < B && !st; ++k)
+    if (uniq[k] && fwrite(pairs + start[k], rec, uniq[k], f) != uniq[k]) st = -2;
+  if (f && fclose(f) != 0 && !st) st = -2;
+  free(pairs);
+  free(start);
+  free(uniq);
+  free(np);
+  if (m_out) *m_out = m;
+  return st;
+}
+
+/* Root (minimum id) of x's set; roots only ever gain smaller parents. */
+static uint32_t uf_root(uint32_t *par, uint32_t x) {
+  for (;;) {
+    const uint32_t p = __atomic_load_n(&par[x], __ATOMIC_RELAXED);
+    if (p == x) return x;
+    const uint32_t gp = __atomic_load_n(&par[p], __ATOMIC_RELAXED);
+    if (gp != p) __atomic_compare_exchange_n(&par[x], &(uint32_t){p}, gp, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
+    x = gp;
+  }
+}
+
+/* count sources (may repeat only when count exceeds the candidates), picked
+ * uniformly among the out-degree > 0 vertices of the largest weakly
+ * connected component (ties: the component with the smallest id). */
+int orc_pick_sources(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
+                     uint32_t count, uint64_t seed, uint32_t *out) {
+  uint32_t *par = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t *size = (uint32_t *)calloc(n, sizeof(uint32_t));
+  if (!par || !size) { free(par); free(size); return -1; }
+#pragma omp parallel for
+  for (int64_t v = 0; v < (int64_t)n; ++v) par[v] = (uint32_t)v;
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t v = 0; v < (int64_t)n; ++v) {
+    for (uint32_t i = np[v]; i < np[v + 1]; ++i) {
+      uint32_t x = (uint32_t)v, y = ed[(size_t)i * stride];
+      for (;;) {
+        x = uf_root(par, x);
+        y = uf_root(par, y);
+        if (x == y) break;
+        if (x < y) { const uint32_t t = x; x = y; y = t; }
+        uint32_t expect = x;  /* hang the larger root under the smaller */
+        if (__atomic_compare_exchange_n(&par[x], &expect, y, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) break;
+      }
+    }
+  }
+  /* parents always have smaller ids, so one ascending pass leaves roots */
+  for (uint32_t v = 0; v < n; ++v) {
+    par[v] = par[par[v]];
+    size[par[v]]++;
+  }
+  uint32_t best = 0;
+  for (uint32_t v = 1; v < n; ++v)
+    if (size[v] > size[best]) best = v;
+  uint32_t *cand = size;  /* sizes are no longer needed */
+  size_t nc = 0;
+  for (uint32_t v = 0; v < n; ++v)
+    if (par[v] == best && np[v + 1] > np[v]) cand[nc++] = v;
+  free(par);
+  par = cand;
+  if (nc == 0) { free(par); return -2; }
+  uint64_t state = sm_fin(seed ^ 0xa54ff53a5f1d36f1ULL);
+  for (uint32_t k = 0; k < count; ++k) {
+    uint32_t v = 0;
+    int tries = 0, dup;
+    do {
+      state += SM_GAMMA;
+      v = par[(uint32_t)(((sm_fin(state) >> 32) * nc) >> 32)];
+      dup = 0;
+      for (uint32_t j = 0; j < k; ++j) dup |= out[j] == v;
+    } while (count <= nc && ++tries < 1000 && dup);
+    out[k] = v;
+  }
+  free(par);
+  return 0;
+}

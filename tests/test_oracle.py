@@ -100,3 +100,46 @@ def test_partition_restatement(orc):
     assert orc.partition(ptr, 12) is None  # vertex 3 has 18 > 10 edges: the reference never ends
     fr, sz = orc.partition(ptr, 100)
     assert fr.tolist() == [0] and sz.tolist() == [5]
+
+
+@pytest.mark.parametrize("scale,weighted,seed", [(10, True, 3), (13, False, 5), (15, True, 24)])
+def test_rmat_writer_matches_engine_generator(native, orc, tmp_path, scale, weighted, seed):
+    """The oracle's R-MAT file (the reference arm's input, made without the
+    engine library) has the same bytes as the engine generator's saved graph,
+    and its source choice is the same."""
+    ext = "bwcsr" if weighted else "bcsr"
+    g = native.Graph.rmat(scale, 16, seed=seed, weighted=weighted, wmax=64)
+    g.save(tmp_path / f"eng.{ext}")
+    m = orc.rmat_write(tmp_path / f"orc.{ext}", scale, 16, seed=seed, weighted=weighted, wmax=64)
+    assert m == g.m
+    assert (tmp_path / f"eng.{ext}").read_bytes() == (tmp_path / f"orc.{ext}").read_bytes()
+    npt, ed = orc.read_csr(tmp_path / f"orc.{ext}")
+    assert np.array_equal(npt, g.node_pointer)
+    src = orc.pick_sources(npt, ed, 16, seed=seed)
+    assert src.tolist() == g.pick_sources(16, seed=seed).tolist()
+
+
+def test_delta_stepping_equals_dijkstra_and_frontier(native, orc):
+    """omp_sssp (delta-stepping) against serial Dijkstra and the bucket-free
+    frontier method, on R-MAT and on a graph with heavy weights."""
+    for g in (native.Graph.rmat(15, 16, seed=11, weighted=True, wmax=64),
+              native.Graph.er(20000, 200000, seed=3, weighted=True, wmax=100000)):
+        for s in g.pick_sources(4, seed=9):
+            ref = orc.run("sssp", g.node_pointer, g.edges, int(s))
+            assert np.array_equal(orc.run("sssp", g.node_pointer, g.edges, int(s), parallel=True), ref)
+            assert np.array_equal(orc.sssp_frontier(g.node_pointer, g.edges, int(s)), ref)
+
+
+def test_reached_edges_multi_source(native, orc):
+    """The bit-parallel reachability count equals one BFS per source (70
+    sources: two calls of 64 and 6), including repeated sources."""
+    g = native.Graph.rmat(13, 8, seed=4, weighted=False)
+    src = np.concatenate([g.pick_sources(68, seed=1), [0, 0]]).astype(np.uint32)
+    deg = g.out_degree().astype(np.uint64)
+    want = [int(deg[orc.run("bfs", g.node_pointer, g.ends, int(s)) != INF].sum()) for s in src]
+    assert orc.reached_edges(g.node_pointer, g.ends, src).tolist() == want
+    gw = native.Graph.rmat(12, 16, seed=4, weighted=True)
+    s2 = gw.pick_sources(5, seed=3)
+    want2 = [int(gw.out_degree()[orc.run("bfs", gw.node_pointer, gw.edges, int(s)) != INF].astype(np.uint64).sum())
+             for s in s2]
+    assert orc.reached_edges(gw.node_pointer, gw.edges, s2).tolist() == want2
