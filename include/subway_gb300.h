@@ -204,7 +204,7 @@ typedef struct sgw_run_stats {
   double ms_device;             /* CUDA-event time of the processing loop       */
   double ms_generate;           /* SGW_OPT_PROFILE: per kernel class totals     */
   double ms_partition;
-  double ms_gather;
+  double ms_gather;             /* the gather kernel (k_gather_v) alone         */
   double ms_relax;
   uint64_t launches;            /* kernels launched by the run                  */
   uint64_t gather_launches;
@@ -212,7 +212,11 @@ typedef struct sgw_run_stats {
   uint64_t generate_launches;
   uint64_t relaxed_edges;       /* edges expanded by the relaxation kernels     */
   uint64_t relaxed_sources;     /* sources whose edges were expanded            */
-  uint64_t reserved[2];
+  uint64_t gather_bytes;        /* host bytes the gather kernel read (the same
+                                   count is written to HBM); h2d_bytes minus
+                                   this is what DMA copies moved                */
+  double ms_stream;             /* SGW_OPT_PROFILE: DMA copies of whole ranges
+                                   and of split-vertex pieces                   */
 } sgw_run_stats;
 
 /* One whole application run: the init loops, the first generate, the

@@ -4,8 +4,8 @@ TEST AND BASELINE INFRASTRUCTURE.  Outputs only under oracle/_ref/ (git-ignored)
 
   oracle/_ref/src/        the reference's shared/ and subway/ sources, copied
                           verbatim from the reference tree when it is present
-                          (this container), so that a GPU machine without the
-                          reference tree can compile them too
+                          (SUBWAY_REFERENCE_TREE), so that a GPU machine
+                          without the reference tree can compile them too
   oracle/_ref/bin/        the ten apps as shipped (bfs-sync ... pr-async)
   oracle/_ref/bin_fixed/  the same apps with the host-gather chunk size
                           rounded up (shared/subgraph_generator.cu:75 divides
@@ -27,7 +27,10 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_TREE = Path("/root/reference")
+# Where the upstream Subway tree is read from when it is present (the build
+# container mounts it there); elsewhere the copy staged under oracle/_ref/src
+# is compiled.
+REF_TREE = Path(os.environ.get("SUBWAY_REFERENCE_TREE", "/root/reference"))
 OUT = HERE / "_ref"
 SRC = OUT / "src"
 OBJ = OUT / "obj"

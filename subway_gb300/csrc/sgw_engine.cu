@@ -64,6 +64,7 @@ struct sgw_engine {
   uint64_t hub_iters = 0;        // single-vertex partitions relaxed (counted on the host)
   uint32_t *d_queue = nullptr, *d_ptr = nullptr;
   uint32_t *d_tflag = nullptr;
+  uint32_t *d_gmask = nullptr;             // generate: keep | clear bits per 16-vertex group
   unsigned long long *d_tagg = nullptr, *d_tincl = nullptr;
   Ctl *d_ctl = nullptr;
   Part *d_parts = nullptr;
@@ -96,10 +97,9 @@ struct sgw_engine {
   const char *h_wsrc = nullptr;            // host view of the weight stream
   uint8_t *d_wbuf[kMaxBuf] = {};           // weight bytes of each edge buffer
   uint32_t rec_bytes = 4;                  // device bytes per edge in a buffer
-  bool registered = false;
   uint32_t *h_packed = nullptr;            // packed transfer copy (weighted graphs)
   size_t packed_bytes = 0;
-  bool packed_registered = false;
+
   bool vec_gather = false;                 // host records readable as aligned 16-B words
   uint32_t cur_streamed = 0;               // partition being relaxed: whole-range buffer
   uint32_t cur_stream_base = 0;            //   and the first edge of that range
@@ -169,7 +169,8 @@ int prof_collect(sgw_engine *e) {
   e->prof_used = 0;
   e->stats.ms_generate += ms[K_GENERATE];
   e->stats.ms_partition += ms[K_PLAN];
-  e->stats.ms_gather += ms[K_GATHER] + ms[K_STREAM];  // transfers of both kinds
+  e->stats.ms_gather += ms[K_GATHER];
+  e->stats.ms_stream += ms[K_STREAM];
   e->stats.ms_relax += ms[K_RELAX];
   // the whole-range copies' own rate: if it falls below what the policy
   // assumes, later runs send compacted edges only
@@ -241,7 +242,7 @@ int read_ctl(sgw_engine *e) {
 enum Family { FAM_INT = 0, FAM_PR = 1 };
 
 struct Layout {
-  size_t off, tflag, tagg, tincl, ctl, mlp, sel;      // common
+  size_t off, tflag, tagg, tincl, ctl, mlp, sel, gmask;  // common
   size_t value, l1, l2, queue, ptr, delta, qpush;     // family
   size_t parts, ranges, rstat, wl, buf[kMaxBuf], total;
   uint64_t cap;
@@ -260,6 +261,7 @@ Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
   L.ctl = take(sizeof(Ctl));
   L.mlp = take(sizeof(__nv_bfloat16) * kMlpParams);
   L.sel = take(sizeof(unsigned long long) * kSelBins);
+  L.gmask = take(4ull * ((n + kGenVPerLane - 1) / kGenVPerLane));
   if (fam == FAM_INT) {
     L.value = take(4ull * n);
     L.l1 = take(n);
@@ -319,6 +321,7 @@ int carve(sgw_engine *e, int fam, uint64_t cap) {
   e->d_tagg = (unsigned long long *)(b + L.tagg);
   e->d_tincl = (unsigned long long *)(b + L.tincl);
   e->d_ctl = (Ctl *)(b + L.ctl);
+  e->d_gmask = (uint32_t *)(b + L.gmask);
   e->d_value = (uint32_t *)(b + L.value);
   e->d_l1 = fam == FAM_INT ? (uint8_t *)(b + L.l1) : nullptr;
   e->d_l2 = fam == FAM_INT ? (uint8_t *)(b + L.l2) : nullptr;
@@ -429,6 +432,7 @@ int launch_generate(sgw_engine *e, int consume) {
   a.tagg = e->d_tagg;
   a.tincl = e->d_tincl;
   a.ctl = e->d_ctl;
+  a.gmask = e->d_gmask;
   e->epoch = (e->epoch + 1) & 0x3fffffffu;
   if (e->epoch == 0) e->epoch = 1;
   a.epoch = e->epoch;
@@ -568,6 +572,7 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
                                                 (uint32_t)q.edge_count);
   CK(cudaGetLastError());
   e->stats.h2d_bytes += q.edge_count * (4ull * e->W + (e->use_w ? 1 : 0));
+  e->stats.gather_bytes += q.edge_count * (4ull * e->W + (e->use_w ? 1 : 0));
   TRY(prof_end(e, s, slot));
   CK(cudaEventRecord(e->ev_ready[b], s));
   e->stats.launches += 1;
@@ -701,10 +706,11 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
   for (uint64_t s = 0; s < deg; s += e->cap) {
     const uint32_t cnt = (uint32_t)std::min<uint64_t>(e->cap, deg - s);
     size_t slot = 0;
-    TRY(prof_begin(e, K_GATHER, e->s_comp, &slot));
+    TRY(prof_begin(e, K_STREAM, e->s_comp, &slot));
     CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->h_src + (hoff + s) * esz, cnt * esz,
                        cudaMemcpyHostToDevice, e->s_comp));
     e->stats.h2d_bytes += cnt * esz;
+    e->stream_bytes += cnt * esz + (e->use_w ? cnt : 0);
     if (e->use_w) {
       CK(cudaMemcpyAsync(e->d_wbuf[b], e->h_wsrc + hoff + s, cnt, cudaMemcpyHostToDevice, e->s_comp));
       e->stats.h2d_bytes += cnt;
@@ -1220,12 +1226,13 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   e->m = g->m;
   e->W = g->weighted ? 2 : 1;
   // weighted records travel as one packed word when (w << bits(n)) | dst fits
-  bool pack = g->weighted && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SPLIT_WEIGHTS)) && pack_bits(g, &e->pbits);
+  const uint32_t wmax = max_weight(g);  // one pass over the records
+  bool pack = g->weighted && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SPLIT_WEIGHTS)) &&
+              pack_bits_for(g, wmax, &e->pbits);
   if (pack) e->W = 1;
   else e->pbits = 0;
   // otherwise weights below 256 travel as their own byte stream
-  e->split = g->weighted && !pack && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SCALAR_GATHER)) &&
-             max_weight(g) < 256;
+  e->split = g->weighted && !pack && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SCALAR_GATHER)) && wmax < 256;
   if (e->split) e->W = 1;
   e->rec_bytes = 4 * e->W + (e->split ? 1 : 0);
   e->nbuf = (o.flags & SGW_OPT_NO_OVERLAP) ? 1 : 2;
@@ -1287,9 +1294,13 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   auto cleanup = [&](int s) { sgw_engine_destroy(e); return s; };
   // The transfer copy: the edge records (packed when they fit) in pinned,
   // mapped host memory from cudaHostAlloc, read in place by the gather
-  // kernels and by DMA copies.  Registering the caller's pages instead makes
-  // DMA from them several times slower on the C2C-attached host.  16 bytes of
-  // padding let the 16-byte vector reads run past the last record.
+  // kernels and by DMA copies.  Ordinary pages written by all host threads
+  // and then registered with cudaHostRegister cost less to set up (0.5 s
+  // against 1.2 s for the 21 GB copy of RMAT-28 on a GB300 host), but the GPU
+  // then reached them through host page-table translations: the plain
+  // schedule's gathers, which touch rows all over the copy, ran at 7-9 GB/s
+  // instead of 130-170 GB/s.  16 bytes of padding let the 16-byte vector
+  // reads run past the last record.
   if (g->m > 0) {
     const size_t rec_bytes = (size_t)e->m * 4 * e->W;
     const size_t ends_alloc = (rec_bytes + 16 + 15) / 16 * 16;
@@ -1302,7 +1313,6 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
       return cleanup(fail(SGW_ECUDA, "cudaHostAlloc(%zu) for the transfer copy: %s", e->packed_bytes,
                           cudaGetErrorString(ce)));
     }
-    e->packed_registered = true;  // owned by the CUDA runtime: cudaFreeHost on destroy
     char *hw = (char *)e->h_packed + ends_alloc;
     if (pack) pack_into(g, e->pbits, e->h_packed);
     else if (e->split) split_into(g, e->h_packed, (uint8_t *)hw);
@@ -1700,6 +1710,7 @@ extern "C" int sgw_generate_noalloc(uint8_t *d_label1, uint8_t *d_label2,
   a.tagg = reinterpret_cast<unsigned long long *>(scratch + kNaAggOff);
   a.tincl = reinterpret_cast<unsigned long long *>(scratch + kNaInclOff);
   a.ctl = ctl;
+  a.gmask = nullptr;
   a.epoch = epoch;
   a.num_tiles = (n + kGenTile - 1) / kGenTile;
   a.consume = consume ? 1 : 0;

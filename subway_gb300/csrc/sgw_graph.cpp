@@ -73,18 +73,26 @@ int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out) {
   return SGW_OK;
 }
 
-bool pack_bits(const sgw_graph *g, uint32_t *nbits) {
+bool pack_bits_for(const sgw_graph *g, uint32_t wmax, uint32_t *nbits) {
   if (!g->weighted || g->m == 0) return false;
   uint32_t nb = 1;
   while (nb < 32 && (uint64_t(1) << nb) < g->n) ++nb;
   if (nb >= 31) return false;
-  const uint32_t *ed = (const uint32_t *)g->edges;
-  uint32_t wmax = 0;
-#pragma omp parallel for reduction(max : wmax)
-  for (int64_t i = 0; i < (int64_t)g->m; ++i) wmax = std::max(wmax, ed[2 * size_t(i) + 1]);
   if ((uint64_t)wmax >= (uint64_t(1) << (32 - nb))) return false;
   *nbits = nb;
   return true;
+}
+
+bool pack_bits(const sgw_graph *g, uint32_t *nbits) { return pack_bits_for(g, max_weight(g), nbits); }
+
+void copy_bytes(void *dst, const void *src, size_t bytes) {
+  const size_t piece = size_t(64) << 20;
+  const int64_t pieces = (int64_t)((bytes + piece - 1) / piece);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < pieces; ++k) {
+    const size_t a = size_t(k) * piece, b = std::min(bytes, a + piece);
+    memcpy((char *)dst + a, (const char *)src + a, b - a);
+  }
 }
 
 void pack_into(const sgw_graph *g, uint32_t nb, uint32_t *p) {
@@ -93,16 +101,7 @@ void pack_into(const sgw_graph *g, uint32_t nb, uint32_t *p) {
   for (int64_t i = 0; i < (int64_t)g->m; ++i) p[i] = (ed[2 * size_t(i) + 1] << nb) | ed[2 * size_t(i)];
 }
 
-void copy_records(const sgw_graph *g, void *out) {
-  const size_t total = size_t(g->m) * g->esz;
-  const size_t piece = size_t(64) << 20;
-  const int64_t pieces = (int64_t)((total + piece - 1) / piece);
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t k = 0; k < pieces; ++k) {
-    const size_t a = size_t(k) * piece, b = std::min(total, a + piece);
-    memcpy((char *)out + a, (const char *)g->edges + a, b - a);
-  }
-}
+void copy_records(const sgw_graph *g, void *out) { copy_bytes(out, g->edges, size_t(g->m) * g->esz); }
 
 uint32_t max_weight(const sgw_graph *g) {
   if (!g->weighted || g->m == 0) return 0;

@@ -40,6 +40,10 @@ int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out);
 bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint32_t *nbits);
 // The same decision and fill into a caller-provided array of m words.
 bool pack_bits(const sgw_graph *g, uint32_t *nbits);
+// The same test given the largest weight (from max_weight).
+bool pack_bits_for(const sgw_graph *g, uint32_t wmax, uint32_t *nbits);
+// Parallel memcpy in 64 MiB pieces.
+void copy_bytes(void *dst, const void *src, size_t bytes);
 void pack_into(const sgw_graph *g, uint32_t nbits, uint32_t *out);
 // Parallel copy of the edge records (m * esz bytes) into out.
 void copy_records(const sgw_graph *g, void *out);

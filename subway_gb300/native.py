@@ -54,7 +54,7 @@ class RunStats(C.Structure):
                 ("launches", C.c_uint64), ("gather_launches", C.c_uint64),
                 ("relax_launches", C.c_uint64), ("generate_launches", C.c_uint64),
                 ("relaxed_edges", C.c_uint64), ("relaxed_sources", C.c_uint64),
-                ("reserved", C.c_uint64 * 2)]
+                ("gather_bytes", C.c_uint64), ("ms_stream", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

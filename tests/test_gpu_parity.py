@@ -248,7 +248,7 @@ def test_engine_matches_reference_golden(gpu):
     """The engine against the reference build's own outputs (tests/golden)."""
     from pathlib import Path
     d = np.load(Path(__file__).resolve().parent / "golden" / "ref_rmat13.npz")
-    scale, ef, seed, wmax, _ = (int(x) for x in d["params"])
+    scale, ef, seed, wmax = (int(x) for x in d["params"][:4])
     gu = gpu.Graph.rmat(scale, ef, seed=seed)
     gw = gpu.Graph.rmat(scale, ef, seed=seed, weighted=True, wmax=wmax)
     engines = {False: gpu.Engine(gu, budget_bytes=36 * gu.n + 96 * 1024 + 20000 * 8),
@@ -269,6 +269,40 @@ def test_engine_matches_reference_golden(gpu):
                 assert np.max(np.abs(vals - ref) / ref) < PR_ACC / PR_INIT, k
         else:
             assert np.array_equal(vals, d[k]), k
+
+
+def test_engine_matches_reference_rmat16(gpu):
+    """BFS-sync and SSSP-sync from source 0 on R-MAT scale 16, whole graph on
+    the device: bit-exact against the fixed reference build's outputs."""
+    from pathlib import Path
+    d = np.load(Path(__file__).resolve().parent / "golden" / "ref_rmat16.npz")
+    scale, ef, seed, wmax = (int(x) for x in d["params"][:4])
+    gu = gpu.Graph.rmat(scale, ef, seed=seed)
+    gw = gpu.Graph.rmat(scale, ef, seed=seed, weighted=True, wmax=wmax)
+    for algo, g in (("bfs", gu), ("sssp", gw)):
+        vals, _ = gpu.Engine(g).run(algo, "sync", 0)
+        assert np.array_equal(vals, d[f"fixed/{algo}-sync/s0"]), algo
+
+
+@pytest.mark.parametrize("policy", ["plain", "learned"])
+def test_engine_matches_reference_rmat24_digests(gpu, policy):
+    """SSSP-async on R-MAT scale 24 under a 1 GB budget (the smaller benchmark
+    workload), 8 sources: each distance array hashes to the fixed reference
+    build's digest."""
+    import hashlib
+    import json
+    from pathlib import Path
+    rep = json.loads((Path(__file__).resolve().parent / "golden" / "ref_rmat24_sssp_async_1gb.json").read_text())
+    g = gpu.Graph.rmat(24, 16, seed=24, weighted=True, wmax=64)
+    assert g.pick_sources(8, seed=24).tolist() == rep["sources"]
+    nb = gpu.sched_buffers(g, 1e9) if policy == "learned" else 0
+    eng = gpu.Engine(g, budget_bytes=1_000_000_000, num_buffers=nb)
+    if policy == "learned":
+        from subway_gb300 import scheduler
+        eng.set_policy("learned", scheduler.load_default(0))
+    for s in rep["sources"]:
+        vals, _ = eng.run("sssp", "async", s)
+        assert hashlib.sha256(vals.tobytes()).hexdigest() == rep["runs"][f"fixed/sssp-async/s{s}"]["sha256"], s
 
 
 @pytest.mark.parametrize("mode", MODES)
