@@ -217,6 +217,7 @@ struct GenArgs {
   unsigned long long *tagg;
   unsigned long long *tincl;
   Ctl *ctl;
+  uint32_t *gmask;           // count/write form: per 16-vertex group, keep bits | clear bits << 16
   uint32_t epoch;
   uint32_t num_tiles;
   int consume;               // sync: labels of queued vertices are cleared
@@ -479,13 +480,45 @@ __device__ __forceinline__ void gen_lane(const GenArgs &a, uint32_t v0, bool ful
   }
 }
 
+// Clears the labels of the lane's vertices in L.clearmask (16-byte stores of
+// the words read by gen_lane when the group is whole).
+__device__ __forceinline__ void gen_clear(const GenArgs &a, uint32_t v0, bool full, const GenLane &L) {
+  if (!L.clearmask) return;
+  uint32_t cw[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    cw[q] = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+      if ((L.clearmask >> (4 * q + b)) & 1u) cw[q] |= 0xffu << (8 * b);
+  }
+  if (full) {
+    *reinterpret_cast<uint4 *>(a.l1 + v0) =
+        make_uint4(L.l1w[0] & ~cw[0], L.l1w[1] & ~cw[1], L.l1w[2] & ~cw[2], L.l1w[3] & ~cw[3]);
+    *reinterpret_cast<uint4 *>(a.l2 + v0) =
+        make_uint4(L.l2w[0] & ~cw[0], L.l2w[1] & ~cw[1], L.l2w[2] & ~cw[2], L.l2w[3] & ~cw[3]);
+  } else {
+    for (uint32_t k = 0; k < kGenVPerLane; ++k)
+      if ((L.clearmask >> k) & 1u) { a.l1[v0 + k] = 0; a.l2[v0 + k] = 0; }
+  }
+}
+
+// Count pass: the selection of every lane's 16 vertices, whose keep and
+// clear bits it records per group (so the write pass reads 4 bytes per 16
+// vertices instead of the labels and values again), the label clearing, and
+// the tile's (count, edges) total.
 __global__ void __launch_bounds__(kGenThreads) k_generate_count(GenArgs a) {
   __shared__ unsigned long long s_warp[kGenThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t tile = blockIdx.x;
   const uint32_t v0 = tile * kGenTile + warp * (32 * kGenRounds) + lane * kGenVPerLane;
+  const bool full = v0 + kGenVPerLane <= a.n;
   GenLane L;
-  if (v0 < a.n) gen_lane(a, v0, v0 + kGenVPerLane <= a.n, L);
+  if (v0 < a.n) {
+    gen_lane(a, v0, full, L);
+    gen_clear(a, v0, full, L);
+    a.gmask[v0 / kGenVPerLane] = L.keepmask | (L.clearmask << 16);
+  }
   const uint32_t seen = __reduce_add_sync(0xffffffffu, L.seen);
   const uint32_t c = __reduce_add_sync(0xffffffffu, L.cnt);
   const uint32_t e = __reduce_add_sync(0xffffffffu, L.edges);
@@ -546,6 +579,8 @@ __global__ void __launch_bounds__(kGenScanThreads) k_generate_scan(GenArgs a) {
   }
 }
 
+// Write pass: the group's keep bits from the count pass, the node pointers
+// of groups that queue a vertex, and the queue / pointer entries.
 __global__ void __launch_bounds__(kGenThreads) k_generate_write(GenArgs a) {
   __shared__ unsigned long long s_warp[kGenThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -553,24 +588,24 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_write(GenArgs a) {
   const uint32_t v0 = tile * kGenTile + warp * (32 * kGenRounds) + lane * kGenVPerLane;
   const bool full = v0 + kGenVPerLane <= a.n;
   GenLane L;
-  if (v0 < a.n) gen_lane(a, v0, full, L);
-  if (L.clearmask) {
-    uint32_t cw[4];
+  if (v0 < a.n) {
+    L.keepmask = a.gmask[v0 / kGenVPerLane] & 0xffffu;
+    if (L.keepmask) {
+      if (full) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      cw[q] = 0;
+        for (int q = 0; q < 4; ++q) {
+          const uint4 p = __ldg(reinterpret_cast<const uint4 *>(a.off + v0) + q);
+          L.o[4 * q] = p.x; L.o[4 * q + 1] = p.y; L.o[4 * q + 2] = p.z; L.o[4 * q + 3] = p.w;
+        }
+        L.o[kGenVPerLane] = __ldg(&a.off[v0 + kGenVPerLane]);
+      } else {
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
-        if ((L.clearmask >> (4 * q + b)) & 1u) cw[q] |= 0xffu << (8 * b);
-    }
-    if (full) {
-      *reinterpret_cast<uint4 *>(a.l1 + v0) =
-          make_uint4(L.l1w[0] & ~cw[0], L.l1w[1] & ~cw[1], L.l1w[2] & ~cw[2], L.l1w[3] & ~cw[3]);
-      *reinterpret_cast<uint4 *>(a.l2 + v0) =
-          make_uint4(L.l2w[0] & ~cw[0], L.l2w[1] & ~cw[1], L.l2w[2] & ~cw[2], L.l2w[3] & ~cw[3]);
-    } else {
+        for (uint32_t k = 0; k <= kGenVPerLane; ++k) L.o[k] = (v0 + k <= a.n) ? __ldg(&a.off[v0 + k]) : 0u;
+      }
+      L.cnt = (uint32_t)__popc(L.keepmask);
+#pragma unroll
       for (uint32_t k = 0; k < kGenVPerLane; ++k)
-        if ((L.clearmask >> k) & 1u) { a.l1[v0 + k] = 0; a.l2[v0 + k] = 0; }
+        if ((L.keepmask >> k) & 1u) L.edges += L.o[k + 1] - L.o[k];
     }
   }
   const uint32_t incl_c = warp_incl_scan(L.cnt, lane);
