@@ -92,6 +92,10 @@ def parse_args(argv=None):
                     help="scale27: BFS, CC, SSWP (and PR with --suite-pr) sync and async on R-MAT scale 27 "
                          "under a 4 GB budget plus an Erdos-Renyi control, each checked against the oracle")
     ap.add_argument("--suite-pr", action="store_true", help="add PageRank (6 GB budget) to the suite")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="one warm-up run and one measured run of --policy (plain or learned) from the first "
+                         "two sources; prints each run's launches per kernel class (for ncu -s / -c) and the "
+                         "measured run's algorithmic bytes")
     ap.add_argument("--ref-time-limit", type=float, default=900.0,
                     help="reference arm: stop starting processes after this many seconds (>= 2 timed)")
     return ap.parse_args(argv)
@@ -331,6 +335,21 @@ def run_ours(a, dist):
                 check["mismatches"] += int(np.count_nonzero(out != ref))
                 check["reached_mismatches"] += int(st["reached_edges"] != want)
             check["checked_sources"] += 1
+        # where tests/golden holds the reference build's own digests for this
+        # workload, the learned schedule's distances are compared with them too
+        import hashlib
+        gold = ROOT / "tests" / "golden" / f"ref_rmat{a.scale}_{a.algo}_{a.mode}_{int(a.budget / 1e9)}gb.json"
+        if "learned" in engines and gold.exists() and a.edge_factor == 16:
+            rep = json.loads(gold.read_text())
+            if f"seed {a.seed}," in rep["graph"] and rep["budget_bytes"] == int(a.budget):
+                hits = 0
+                for s in rep["sources"]:
+                    engines["learned"].run(a.algo, a.mode, s, out=out)
+                    key = next(k for k in rep["runs"] if k.startswith("fixed/") and k.endswith(f"/s{s}"))
+                    hits += hashlib.sha256(out.tobytes()).hexdigest() == rep["runs"][key]["sha256"]
+                check["reference_digests"] = {"checked": len(rep["sources"]), "equal": hits,
+                                              "fixture": gold.name}
+                check["mismatches"] += len(rep["sources"]) - hits
         cpu = {"value": round(reached_cpu / secs / 1e9, 4), "unit": "GTEPS", "cores": oracle.num_threads(),
                "kind": "port",
                "sample": f"{check['checked_sources']} full {a.algo} runs of the OpenMP oracle "
@@ -447,6 +466,42 @@ def run_ours(a, dist):
     if dist.rank == 0 and cpu:
         line["cpu_baseline"] = cpu
     return line
+
+
+# ---- one run for a profiler ------------------------------------------------------------
+def run_profile(a, dist):
+    """What an ncu capture of one run needs: the launch counts of the warm-up
+    run (ncu -s) and of the measured run (ncu -c) per kernel class, and the
+    measured run's algorithmic bytes to compare with the captured DRAM bytes.
+    Per generate step the integer family launches k_generate_count, _scan and
+    _write; per relaxation pass k_relax_warp and k_relax_chunks."""
+    import numpy as np
+
+    from subway_gb300 import native as N
+    from subway_gb300 import scheduler
+
+    policy = "plain" if a.policy == "plain" else "learned"
+    weighted = weighted_algo(a.algo)
+    g = N.Graph.rmat(a.scale, a.edge_factor, seed=a.seed, weighted=weighted, wmax=64)
+    src = [int(s) for s in g.pick_sources(2, seed=a.seed)]
+    nb = (a.num_buffers or N.sched_buffers(g, a.budget)) if policy == "learned" else 0
+    e = N.Engine(g, budget_bytes=int(a.budget), device=dist.local, flags=N.OPT_PROFILE, num_buffers=nb,
+                 gather_ctas=a.gather_ctas, tile_degree_max=a.tile_degree_max, chunk_edges=a.chunk_edges)
+    if policy == "learned":
+        e.set_policy("learned", scheduler.load_default(dist.local))
+    out = np.empty(g.n, np.uint32)
+    _, w = e.run(a.algo, a.mode, src[1], out=out)
+    _, st = e.run(a.algo, a.mode, src[0], out=out)
+    esz = transfer_record_bytes(g.n, weighted, a.no_pack)
+    keys = ("gather_launches", "relax_launches", "generate_launches", "launches")
+    return {"profile_run": policy, "workload": workload_config(a)["workload"],
+            "warm": {k: w[k] for k in keys},
+            "run": {k: st[k] for k in keys + ("ms_gather", "ms_relax", "ms_generate", "ms_device", "relaxed_edges",
+                                              "relaxed_sources", "active_vertices", "gather_bytes", "h2d_bytes")},
+            "algorithmic_bytes": {"gather": st["gather_bytes"],
+                                  "relax": st["relaxed_sources"] * 17 + st["relaxed_edges"] * (esz + 4),
+                                  "generate": st["generate_launches"] * 2 * g.n + st["active_vertices"] * 16},
+            "record_bytes": esz}
 
 
 # ---- the scale-27 suite --------------------------------------------------------------
@@ -639,7 +694,9 @@ def run_reference(a, dist):
 def main():
     a = parse_args()
     dist = Dist(a.gpus)
-    if a.suite:
+    if a.profile_run:
+        line = run_profile(a, dist)
+    elif a.suite:
         line = run_suite(a, dist)
     elif a.impl == "reference":
         if dist.rank != 0:
