@@ -233,12 +233,11 @@ def probe_link(N, dev):
 
 
 # DRAM bytes (read + write) per algorithmic byte of each kernel class, from
-# one-kernel ncu captures on RMAT-24 under a 1 GB budget (cold caches: ncu
-# empties them before each launch):
-# profiles/k_gather_v_rmat24_sssp_async_1gb.md, k_relax_warp_rmat24_sssp_async_1gb.md,
-# k_generate_rmat24_sssp_async_1gb.md.  A full-size launch's traffic is the
-# ratio times its algorithmic bytes (estimated, not counted live).
-DRAM_PER_ALGO_BYTE = {"gather": 1.21, "relax": 0.93, "generate": 2.36}
+# one-kernel-class ncu captures over one measured RMAT-24 / 1 GB run
+# (profiles/dram_per_class_rmat24_sssp_async_1gb.md; ncu empties the caches
+# before each launch, so these are cold-cache figures).  A full-size launch's
+# traffic is the ratio times its algorithmic bytes: an estimate, not a count.
+DRAM_PER_ALGO_BYTE = {"gather": 0.73, "relax": 1.06, "generate": 2.23}
 
 
 def run_ours(a, dist):
