@@ -117,6 +117,14 @@ void sgw_graph_free(sgw_graph *g);
  * (5 bytes per edge; BFS/CC/PR move only the destinations).  This flag uses
  * that split form even where the packed word would fit. */
 #define SGW_OPT_SPLIT_WEIGHTS 0x20u
+/* sgw_batch_create: a batch runs either as one cooperative launch whose
+ * blocks loop over the iterations behind grid barriers (the persistent form;
+ * a barrier waits at most 2 s, after which the run returns SGW_ETIMEOUT), or
+ * as a CUDA graph whose conditional WHILE node repeats one iteration's
+ * kernels.  By default SSSP batches take the persistent form and BFS batches
+ * the graph (measured best); these flags force one form for both. */
+#define SGW_OPT_BATCH_PERSISTENT 0x40u
+#define SGW_OPT_BATCH_GRAPH 0x80u
 /* sched_flags: the learned policy's inner cap also covers compacted ranges */
 #define SGW_SCHED_CAP_COMPACT 0x1u
 /* sched_flags: transfer active vertices that cannot push, as the reference's
@@ -416,6 +424,20 @@ int sgw_batch_device_bytes(const sgw_batch *b, uint64_t *bytes);
  * pinned buffer (faster: no pageable copy), see sgw_batch_results. */
 int sgw_batch_run(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc,
                   uint32_t *out, sgw_batch_stats *stats);
+/* sgw_batch_run with 16-bit answers (no reference counterpart): distances or
+ * levels as uint16, unreached = 0xffff, half the bytes copied to the host
+ * (the copy-out bounds a server on large graphs).  out: nsrc x n uint16,
+ * or NULL to leave them in the batch's pinned buffer (sgw_batch_results,
+ * read as uint16).  A reached value of 0xffff or more returns SGW_ERANGE
+ * (the answers are then not usable; run sgw_batch_run). */
+int sgw_batch_run_u16(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc,
+                      uint16_t *out, sgw_batch_stats *stats);
+/* Failure-path check of the persistent form (no reference counterpart): runs
+ * its kernel once with grid barriers that wait for one block more than the
+ * launch has, so every wait runs out after wait_ns (1 ns .. 1 s).  Returns
+ * SGW_ETIMEOUT when the kernel gave up and the device stayed usable; the
+ * batch object can be used again afterwards. */
+int sgw_batch_check_wait_timeout(sgw_batch *b, uint64_t wait_ns);
 /* The batch's pinned result buffer (lanes x n, lane-major), valid until the
  * next sgw_batch_run or sgw_batch_destroy. */
 int sgw_batch_results(const sgw_batch *b, const uint32_t **results);

@@ -69,7 +69,7 @@ __global__ void k_b_seed(const uint32_t *src, uint32_t nsrc, uint32_t *dist, uns
     atomicOr(&next[s], 1ull << l);
     atomicOr(&seen[s], 1ull << l);
   }
-  if (l == 0) { ctr[0] = 0; ctr[1] = 0; ctr[2] = 0; ctr[3] = 0; }
+  if (l < 16) ctr[l] = 0;
 }
 
 __global__ void k_b_reset(uint32_t *ctr) {
@@ -77,10 +77,24 @@ __global__ void k_b_reset(uint32_t *ctr) {
   ctr[1] = 0;
 }
 
-__global__ void __launch_bounds__(kBThreads) k_b_frontier(uint32_t n, const uint32_t *__restrict__ off,
-                                                          unsigned long long *cur, unsigned long long *next,
-                                                          BItem *items, uint32_t cap, uint32_t *ctr,
-                                                          uint32_t chunk) {
+// Loads that follow writes made earlier in the same launch (the persistent
+// form runs every phase in one kernel) go through L2 (__ldcg): L1 and the
+// read-only path are not kept coherent within a kernel.
+__device__ __forceinline__ BItem b_item(const BItem *items, uint32_t i) {
+  const uint4 v = __ldcg(reinterpret_cast<const uint4 *>(items) + i);
+  BItem it;
+  it.u = v.x;
+  it.e0 = v.y;
+  it.cnt = v.z;
+  it.pad = v.w;
+  return it;
+}
+
+// Frontier phase.  ctr[0]: work items appended, ctr[1]: frontier vertices;
+// err: set to 1 when the item list overflows.
+__device__ __forceinline__ void b_frontier(uint32_t n, const uint32_t *__restrict__ off, unsigned long long *cur,
+                                           unsigned long long *next, BItem *items, uint32_t cap, uint32_t *ctr,
+                                           uint32_t chunk, uint32_t *err) {
   const int lane = threadIdx.x & 31;
   const uint32_t stride = gridDim.x * blockDim.x;
   // loop bound rounded up to whole warps so every lane reaches the shuffles
@@ -89,7 +103,7 @@ __global__ void __launch_bounds__(kBThreads) k_b_frontier(uint32_t n, const uint
     uint32_t nch = 0, deg = 0, e0 = 0;
     bool act = false;
     if (v < n) {
-      const unsigned long long m = next[v];
+      const unsigned long long m = __ldcg(&next[v]);
       if (m) {
         act = true;
         cur[v] = m;
@@ -121,32 +135,37 @@ __global__ void __launch_bounds__(kBThreads) k_b_frontier(uint32_t n, const uint
         it.pad = 0;
         items[base + c] = it;
       } else {
-        atomicExch(&ctr[3], 1u);
+        atomicExch(err, 1u);
       }
     }
   }
 }
 
+__global__ void __launch_bounds__(kBThreads) k_b_frontier(uint32_t n, const uint32_t *__restrict__ off,
+                                                          unsigned long long *cur, unsigned long long *next,
+                                                          BItem *items, uint32_t cap, uint32_t *ctr,
+                                                          uint32_t chunk) {
+  b_frontier(n, off, cur, next, items, cap, ctr, chunk, &ctr[3]);
+}
+
+// Distance-lane relaxation phase over the nitems work items.
 template <bool SSSP, int W, int L>
-__global__ void __launch_bounds__(kBThreads) k_b_relax(const BItem *__restrict__ items, const uint32_t *ctr,
-                                                       uint32_t cap, const uint32_t *__restrict__ edges,
-                                                       uint32_t pbits, uint32_t *dist,
-                                                       const unsigned long long *__restrict__ cur,
-                                                       unsigned long long *next) {
+__device__ __forceinline__ void b_relax(const BItem *items, uint32_t nitems,
+                                        const uint32_t *__restrict__ edges, uint32_t pbits, uint32_t *dist,
+                                        const unsigned long long *cur, unsigned long long *next) {
   const int lane = threadIdx.x & 31;
-  const uint32_t nitems = min(ctr[0], cap);
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   const uint32_t dmask = pbits ? ((1u << pbits) - 1u) : 0xffffffffu;
   for (uint32_t i = gw; i < nitems; i += nw) {
-    const BItem it = items[i];
-    const unsigned long long mask = cur[it.u];
+    const BItem it = b_item(items, i);
+    const unsigned long long mask = __ldcg(&cur[it.u]);
 #pragma unroll
     for (int h = 0; h < L / 32; ++h) {
       const uint32_t bits = (uint32_t)(mask >> (32 * h));
       if (bits == 0) continue;
       const bool active = (bits >> lane) & 1u;
-      const uint32_t du = active ? dist[(size_t)it.u * L + 32 * h + lane] : kBInf;
+      const uint32_t du = active ? __ldcg(&dist[(size_t)it.u * L + 32 * h + lane]) : kBInf;
       for (uint32_t c = 0; c < it.cnt; c += 32) {
         // lane k loads edge c + k; the warp then walks them together
         uint32_t rd = 0, rw = 0;
@@ -172,7 +191,7 @@ __global__ void __launch_bounds__(kBThreads) k_b_relax(const BItem *__restrict__
           }
 #pragma unroll
           for (int q = 0; q < kBUnroll; ++q)
-            seen[q] = (active && k0 + q < cnt) ? dist[(size_t)dst[q] * L + 32 * h + lane] : 0u;
+            seen[q] = (active && k0 + q < cnt) ? __ldcg(&dist[(size_t)dst[q] * L + 32 * h + lane]) : 0u;
 #pragma unroll
           for (int q = 0; q < kBUnroll; ++q) {
             if (k0 + q >= cnt) break;  // uniform across the warp
@@ -196,6 +215,15 @@ __global__ void __launch_bounds__(kBThreads) k_b_relax(const BItem *__restrict__
   }
 }
 
+template <bool SSSP, int W, int L>
+__global__ void __launch_bounds__(kBThreads) k_b_relax(const BItem *__restrict__ items, const uint32_t *ctr,
+                                                       uint32_t cap, const uint32_t *__restrict__ edges,
+                                                       uint32_t pbits, uint32_t *dist,
+                                                       const unsigned long long *__restrict__ cur,
+                                                       unsigned long long *next) {
+  b_relax<SSSP, W, L>(items, min(ctr[0], cap), edges, pbits, dist, cur, next);
+}
+
 // BFS, bit-parallel over the lanes (multi-source BFS): a vertex's 64-bit
 // `seen` mask holds the queries that have reached it.  Lane k of the warp
 // takes edge c + k of the item; one atomicOr claims, for every query whose
@@ -203,29 +231,120 @@ __global__ void __launch_bounds__(kBThreads) k_b_relax(const BItem *__restrict__
 // those get level = iteration + 1 and join the next frontier.  Each (vertex,
 // query) bit is claimed exactly once, so the levels are the BFS levels.
 template <int W, int L>
+__device__ __forceinline__ void b_bfs_relax(const BItem *items, uint32_t nitems, uint32_t level,
+                                            const uint32_t *__restrict__ edges, uint32_t pbits, uint32_t *dist,
+                                            const unsigned long long *cur, unsigned long long *next,
+                                            unsigned long long *seen) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t dmask = pbits ? ((1u << pbits) - 1u) : 0xffffffffu;
+  for (uint32_t i = gw; i < nitems; i += nw) {
+    const BItem it = b_item(items, i);
+    const unsigned long long f = __ldcg(&cur[it.u]);
+    if (f == 0ull) continue;
+    for (uint32_t c = lane; c < it.cnt; c += 32) {
+      const size_t e = (size_t)it.e0 + c;
+      const uint32_t dst = W == 1 ? (edges[e] & dmask) : edges[2 * e];
+      if ((__ldcg(&seen[dst]) & f) == f) continue;  // every query here has been there (a stale read only costs the atomic)
+      const unsigned long long fresh = f & ~atomicOr(&seen[dst], f);
+      if (fresh == 0ull) continue;
+      atomicOr(&next[dst], fresh);
+      for (unsigned long long m = fresh; m; m &= m - 1) dist[(size_t)dst * L + (__ffsll((long long)m) - 1)] = level;
+    }
+  }
+}
+
+template <int W, int L>
 __global__ void __launch_bounds__(kBThreads) k_b_bfs_relax(const BItem *__restrict__ items, const uint32_t *ctr,
                                                            uint32_t cap, const uint32_t *__restrict__ edges,
                                                            uint32_t pbits, uint32_t *dist,
                                                            const unsigned long long *__restrict__ cur,
                                                            unsigned long long *next, unsigned long long *seen) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t nitems = min(ctr[0], cap);
-  const uint32_t level = ctr[2] + 1;
-  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  const uint32_t dmask = pbits ? ((1u << pbits) - 1u) : 0xffffffffu;
-  for (uint32_t i = gw; i < nitems; i += nw) {
-    const BItem it = items[i];
-    const unsigned long long f = cur[it.u];
-    if (f == 0ull) continue;
-    for (uint32_t c = lane; c < it.cnt; c += 32) {
-      const size_t e = (size_t)it.e0 + c;
-      const uint32_t dst = W == 1 ? (edges[e] & dmask) : edges[2 * e];
-      if ((seen[dst] & f) == f) continue;  // every query here has been there (a stale read only costs the atomic)
-      const unsigned long long fresh = f & ~atomicOr(&seen[dst], f);
-      if (fresh == 0ull) continue;
-      atomicOr(&next[dst], fresh);
-      for (unsigned long long m = fresh; m; m &= m - 1) dist[(size_t)dst * L + (__ffsll((long long)m) - 1)] = level;
+  b_bfs_relax<W, L>(items, min(ctr[0], cap), ctr[2] + 1, edges, pbits, dist, cur, next, seen);
+}
+
+// ---- persistent form -----------------------------------------------------------
+// One cooperative launch runs every iteration of a batch: frontier phase,
+// grid barrier, relaxation phase, grid barrier, and the loop test, all on the
+// device.  Counter words (ctr): [0..3] as in the graph loop (items, frontier,
+// iterations, error), [4..7] the items / frontier counts of even and odd
+// iterations (the next iteration's pair is cleared during the relaxation
+// phase), [8] barrier arrivals, [9] barrier generation.  A barrier waits at
+// most wait_ns (GPU global timer); a block that gives up records error 4 and
+// returns, and every other block then gives up at its next barrier, so a lost
+// block ends the kernel with an error instead of a hang.
+struct BPersist {
+  uint32_t n, cap, chunk, pbits, max_iters, expect_blocks;
+  unsigned long long wait_ns;
+  const uint32_t *off, *edges;
+  uint32_t *dist, *ctr;
+  unsigned long long *cur, *next, *seen;
+  BItem *items;
+};
+
+__device__ __forceinline__ unsigned long long b_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier with a bounded wait; false once any block has given up.
+__device__ bool b_grid_sync(const BPersist &a) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t *gen = a.ctr + 9;
+    const uint32_t g = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(a.ctr + 8, 1u) == a.expect_blocks - 1) {
+      a.ctr[8] = 0;
+      __threadfence();
+      atomicAdd(a.ctr + 9, 1u);
+    } else {
+      const unsigned long long t0 = b_now();
+      while (*gen == g) {
+        if (b_now() - t0 > a.wait_ns) {
+          atomicExch(a.ctr + 3, 4u);
+          ok = 0;
+          break;
+        }
+        __nanosleep(200);
+      }
+    }
+    __threadfence();
+    if (*(volatile uint32_t *)(a.ctr + 3) == 4u) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <bool SSSP, int W, int L>
+__global__ void __launch_bounds__(kBThreads) k_b_persist(BPersist a) {
+  for (uint32_t it = 0;; ++it) {
+    uint32_t *c = a.ctr + 4 + 2 * (it & 1u);
+    b_frontier(a.n, a.off, a.cur, a.next, a.items, a.cap, c, a.chunk, a.ctr + 3);
+    if (!b_grid_sync(a)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      uint32_t *cn = a.ctr + 4 + 2 * ((it + 1) & 1u);
+      cn[0] = 0;
+      cn[1] = 0;
+    }
+    const uint32_t nitems = min(*(volatile uint32_t *)c, a.cap);
+    if (SSSP) b_relax<true, W, L>(a.items, nitems, a.edges, a.pbits, a.dist, a.cur, a.next);
+    else b_bfs_relax<W, L>(a.items, nitems, it + 1, a.edges, a.pbits, a.dist, a.cur, a.next, a.seen);
+    if (!b_grid_sync(a)) return;
+    const uint32_t frontier = *(volatile uint32_t *)(c + 1);
+    const uint32_t err = *(volatile uint32_t *)(a.ctr + 3);
+    const bool more = frontier > 0 && err == 0;
+    if (!more || it + 1 >= a.max_iters) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ctr[2] = it + 1;
+        if (more) a.ctr[3] = 2;  // iteration limit
+      }
+      return;
     }
   }
 }
@@ -240,7 +359,8 @@ __global__ void k_b_cond(cudaGraphConditionalHandle handle, uint32_t *ctr, uint3
 
 // out[l * n + v - v0] = dist[v * L + l] for v in [v0, v0 + len), l < nsrc.
 template <int L>
-__global__ void k_b_transpose(const uint32_t *dist, uint32_t v0, uint32_t len, uint32_t nsrc, uint32_t *out) {
+__global__ void k_b_transpose(const uint32_t *dist, uint32_t v0, uint32_t len, uint32_t nsrc, uint32_t *out,
+                              uint32_t *) {
   __shared__ uint32_t tile[32][L + 1];
   const uint32_t vb = blockIdx.x * 32;
   for (uint32_t i = threadIdx.x; i < 32 * L; i += blockDim.x) {
@@ -252,6 +372,31 @@ __global__ void k_b_transpose(const uint32_t *dist, uint32_t v0, uint32_t len, u
     const uint32_t l = i / 32, r = i % 32;
     if (l < nsrc && vb + r < len) out[(size_t)l * len + vb + r] = tile[r][l];
   }
+}
+
+// 16-bit answers: unreached (kBInf) becomes 0xffff; a reached distance that
+// does not fit below 0xffff sets *overflow (the run then reports SGW_ERANGE).
+template <int L>
+__global__ void k_b_transpose16(const uint32_t *dist, uint32_t v0, uint32_t len, uint32_t nsrc, uint16_t *out,
+                                uint32_t *overflow) {
+  __shared__ uint32_t tile[32][L + 1];
+  const uint32_t vb = blockIdx.x * 32;
+  for (uint32_t i = threadIdx.x; i < 32 * L; i += blockDim.x) {
+    const uint32_t r = i / L, l = i % L;
+    tile[r][l] = (vb + r < len) ? dist[(size_t)(v0 + vb + r) * L + l] : 0;
+  }
+  __syncthreads();
+  bool over = false;
+  for (uint32_t i = threadIdx.x; i < 32 * L; i += blockDim.x) {
+    const uint32_t l = i / 32, r = i % 32;
+    if (l < nsrc && vb + r < len) {
+      uint32_t v = tile[r][l];
+      if (v == kBInf) v = 0xffffu;
+      else if (v >= 0xffffu) { over = true; v = 0xfffeu; }
+      out[(size_t)l * len + vb + r] = (uint16_t)v;
+    }
+  }
+  if (over) atomicExch(overflow, 1u);
 }
 
 }  // namespace
@@ -278,6 +423,7 @@ struct sgw_batch {
   cudaGraph_t graph[2] = {nullptr, nullptr};        // BFS, SSSP
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   uint32_t max_iters = 0;
+  int form = 0;                   // 0: by algorithm, 1: persistent, 2: graph loop
 };
 
 namespace {
@@ -330,6 +476,66 @@ int build_graph(sgw_batch *b) {
   return SGW_OK;
 }
 
+// Launches the persistent kernel with as many blocks as fit on the device at
+// once (the cooperative launch refuses more), so every block reaches the
+// grid barriers.  extra_blocks > 0 makes each barrier wait for blocks that
+// do not exist (the wait-limit check).
+template <bool SSSP, int W, int L>
+int launch_persist_t(sgw_batch *b, uint32_t extra_blocks, unsigned long long wait_ns) {
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_b_persist<SSSP, W, L>, kBThreads, 0));
+  if (per_sm < 1) return sgw::fail(SGW_ECUDA, "persistent batch kernel does not fit on an SM");
+  const uint32_t grid = (uint32_t)b->num_sms * (uint32_t)std::min(per_sm, 8);
+  BPersist a;
+  a.n = b->n;
+  a.cap = b->items_cap;
+  a.chunk = b->chunk;
+  a.pbits = b->pbits;
+  a.max_iters = b->max_iters;
+  a.expect_blocks = grid + extra_blocks;
+  a.wait_ns = wait_ns;
+  a.off = b->d_off;
+  a.edges = b->d_edges;
+  a.dist = b->d_dist;
+  a.ctr = b->d_ctr;
+  a.cur = b->d_cur;
+  a.next = b->d_next;
+  a.seen = b->d_seen;
+  a.items = b->d_items;
+  void *args[] = {&a};
+  CK(cudaLaunchCooperativeKernel((const void *)k_b_persist<SSSP, W, L>, dim3(grid), dim3(kBThreads), args, 0,
+                                 b->s));
+  return SGW_OK;
+}
+
+int launch_persist(sgw_batch *b, bool sssp, uint32_t extra_blocks, unsigned long long wait_ns) {
+  if (b->lanes == 64) {
+    if (b->W == 1) return sssp ? launch_persist_t<true, 1, 64>(b, extra_blocks, wait_ns)
+                               : launch_persist_t<false, 1, 64>(b, extra_blocks, wait_ns);
+    return sssp ? launch_persist_t<true, 2, 64>(b, extra_blocks, wait_ns)
+                : launch_persist_t<false, 2, 64>(b, extra_blocks, wait_ns);
+  }
+  if (b->W == 1) return sssp ? launch_persist_t<true, 1, 32>(b, extra_blocks, wait_ns)
+                             : launch_persist_t<false, 1, 32>(b, extra_blocks, wait_ns);
+  return sssp ? launch_persist_t<true, 2, 32>(b, extra_blocks, wait_ns)
+              : launch_persist_t<false, 2, 32>(b, extra_blocks, wait_ns);
+}
+
+// A grid barrier waits at most this long before the kernel gives up; a
+// barrier of a healthy run waits for the slowest block of one phase (well
+// under 100 ms on the largest graphs measured).
+constexpr unsigned long long kBarrierWaitNs = 2000000000ull;
+
+int batch_run(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc, void *out, uint32_t answer_bytes,
+              sgw_batch_stats *stats, bool persistent, uint32_t extra_blocks, unsigned long long wait_ns);
+
+// Default form per algorithm, measured on R-MAT 22-26 with 64 queries: the
+// persistent kernel runs SSSP batches 2-9% faster than the graph loop and BFS
+// batches within 4% either way, so SSSP takes it and BFS keeps the graph.
+bool use_persistent(const sgw_batch *b, int algo) {
+  return b->form == 1 || (b->form == 0 && algo == SGW_SSSP);
+}
+
 }  // namespace
 
 extern "C" {
@@ -356,6 +562,22 @@ int sgw_batch_create(const sgw_graph *g, const sgw_engine_opts *opts, uint32_t l
   b->m = g->m;
   b->lanes = lanes;
   b->chunk = o.chunk_edges ? o.chunk_edges : 256;
+  if ((o.flags & SGW_OPT_BATCH_PERSISTENT) && (o.flags & SGW_OPT_BATCH_GRAPH)) {
+    delete b;
+    return sgw::fail(SGW_EINVAL, "SGW_OPT_BATCH_PERSISTENT and SGW_OPT_BATCH_GRAPH exclude each other");
+  }
+  b->form = (o.flags & SGW_OPT_BATCH_PERSISTENT) ? 1 : (o.flags & SGW_OPT_BATCH_GRAPH) ? 2 : 0;
+  {
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, o.device) != cudaSuccess || !coop) {
+      cudaGetLastError();
+      if (b->form == 1) {
+        delete b;
+        return sgw::fail(SGW_EINVAL, "device %d has no cooperative launch", o.device);
+      }
+      b->form = 2;
+    }
+  }
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, o.device) != cudaSuccess) { delete b; return sgw::fail(SGW_ECUDA, "props"); }
   b->num_sms = prop.multiProcessorCount;
@@ -448,6 +670,31 @@ int sgw_batch_device_bytes(const sgw_batch *b, uint64_t *bytes) {
 int sgw_batch_run(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc, uint32_t *out,
                   sgw_batch_stats *stats) {
   sgw::clear_error();
+  if (!b) return sgw::fail(SGW_EINVAL, "null argument");
+  return batch_run(b, algo, sources, nsrc, out, 4, stats, use_persistent(b, algo), 0, kBarrierWaitNs);
+}
+
+int sgw_batch_run_u16(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc, uint16_t *out,
+                      sgw_batch_stats *stats) {
+  sgw::clear_error();
+  if (!b) return sgw::fail(SGW_EINVAL, "null argument");
+  return batch_run(b, algo, sources, nsrc, out, 2, stats, use_persistent(b, algo), 0, kBarrierWaitNs);
+}
+
+int sgw_batch_check_wait_timeout(sgw_batch *b, uint64_t wait_ns) {
+  sgw::clear_error();
+  if (!b) return sgw::fail(SGW_EINVAL, "null argument");
+  if (wait_ns == 0 || wait_ns > 1000000000ull) return sgw::fail(SGW_EINVAL, "wait_ns outside 1..1e9");
+  const uint32_t src = 0;
+  return batch_run(b, SGW_BFS, &src, 1, nullptr, 4, nullptr, true, 1, wait_ns);
+}
+
+}  // extern "C"
+
+namespace {
+
+int batch_run(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc, void *out, uint32_t answer_bytes,
+              sgw_batch_stats *stats, bool persistent, uint32_t extra_blocks, unsigned long long wait_ns) {
   if (!b || !sources) return sgw::fail(SGW_EINVAL, "null argument");
   if (!out) out = b->h_out;  // results stay in the batch's pinned buffer
   if (nsrc == 0 || nsrc > b->lanes) return sgw::fail(SGW_ERANGE, "1..%u sources per batch", b->lanes);
@@ -464,22 +711,37 @@ int sgw_batch_run(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc
   if (b->lanes == 64) k_b_seed<64><<<1, 64, 0, b->s>>>(b->d_src, nsrc, b->d_dist, b->d_next, b->d_seen, b->d_ctr);
   else k_b_seed<32><<<1, 64, 0, b->s>>>(b->d_src, nsrc, b->d_dist, b->d_next, b->d_seen, b->d_ctr);
   CK(cudaGetLastError());
-  CK(cudaGraphLaunch(b->exec[algo == SGW_SSSP ? 1 : 0], b->s));
+  if (persistent) {
+    const int st = launch_persist(b, algo == SGW_SSSP, extra_blocks, wait_ns);
+    if (st != SGW_OK) return st;
+  } else {
+    CK(cudaGraphLaunch(b->exec[algo == SGW_SSSP ? 1 : 0], b->s));
+  }
   CK(cudaEventRecord(b->t1, b->s));
   // lane-major results, staged through a transposed device tile
+  const size_t ab = answer_bytes;
+  char *outb = static_cast<char *>(out);
   for (uint32_t v0 = 0; v0 < b->n; v0 += b->stage_vertices) {
     const uint32_t len = std::min(b->stage_vertices, b->n - v0);
     const uint32_t blocks = (len + 31) / 32;
-    if (b->lanes == 64) k_b_transpose<64><<<blocks, 256, 0, b->s>>>(b->d_dist, v0, len, nsrc, b->d_stage);
-    else k_b_transpose<32><<<blocks, 256, 0, b->s>>>(b->d_dist, v0, len, nsrc, b->d_stage);
+    uint16_t *st16 = reinterpret_cast<uint16_t *>(b->d_stage);
+    if (ab == 2) {
+      if (b->lanes == 64) k_b_transpose16<64><<<blocks, 256, 0, b->s>>>(b->d_dist, v0, len, nsrc, st16, b->d_ctr + 10);
+      else k_b_transpose16<32><<<blocks, 256, 0, b->s>>>(b->d_dist, v0, len, nsrc, st16, b->d_ctr + 10);
+    } else {
+      if (b->lanes == 64) k_b_transpose<64><<<blocks, 256, 0, b->s>>>(b->d_dist, v0, len, nsrc, b->d_stage, nullptr);
+      else k_b_transpose<32><<<blocks, 256, 0, b->s>>>(b->d_dist, v0, len, nsrc, b->d_stage, nullptr);
+    }
     CK(cudaGetLastError());
-    CK(cudaMemcpy2DAsync(out + v0, 4ull * b->n, b->d_stage, 4ull * len, 4ull * len, nsrc,
+    CK(cudaMemcpy2DAsync(outb + ab * v0, ab * b->n, b->d_stage, ab * len, ab * len, nsrc,
                          cudaMemcpyDeviceToHost, b->s));
   }
-  CK(cudaMemcpyAsync(b->h_ctr, b->d_ctr, 16, cudaMemcpyDeviceToHost, b->s));
+  CK(cudaMemcpyAsync(b->h_ctr, b->d_ctr, 64, cudaMemcpyDeviceToHost, b->s));
   CK(cudaStreamSynchronize(b->s));
   if (b->h_ctr[3] == 1) return sgw::fail(SGW_ERANGE, "work item list overflow");
   if (b->h_ctr[3] == 2) return sgw::fail(SGW_ETIMEOUT, "iteration limit reached");
+  if (b->h_ctr[3] == 4) return sgw::fail(SGW_ETIMEOUT, "grid barrier wait timed out");
+  if (b->h_ctr[10]) return sgw::fail(SGW_ERANGE, "a distance does not fit 16 bits: use sgw_batch_run");
   if (stats) {
     float ms = 0;
     cudaEventElapsedTime(&ms, b->t0, b->t1);
@@ -487,9 +749,10 @@ int sgw_batch_run(sgw_batch *b, int algo, const uint32_t *sources, uint32_t nsrc
     stats->queries = nsrc;
     stats->ms_device = ms;
     stats->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
-    stats->d2h_bytes = 4ull * b->n * nsrc;
+    stats->d2h_bytes = ab * b->n * nsrc;
   }
   return SGW_OK;
 }
 
-}  // extern "C"
+}  // namespace
+

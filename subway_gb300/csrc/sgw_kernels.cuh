@@ -817,6 +817,27 @@ __device__ __forceinline__ uint32_t last_le(const uint32_t *a, uint32_t len, uin
   return lo - 1;
 }
 
+// Last queue index i in [lo, hi) with ptr[i] - edge_from <= target, found by
+// one warp in 32-way steps (about five dependent loads for 2^24 entries
+// instead of one per halving).  ptr is non-decreasing and
+// ptr[lo] - edge_from <= target.  Every lane returns the answer.
+__device__ __forceinline__ uint32_t warp_last_le(const uint32_t *__restrict__ ptr, uint32_t lo, uint32_t hi,
+                                                 uint32_t edge_from, uint32_t target, int lane) {
+  while (hi - lo > 32u) {
+    const uint32_t step = (hi - lo + 31u) / 32u;
+    const uint32_t idx = lo + (uint32_t)lane * step;
+    const bool le = idx < hi && ptr[idx] - edge_from <= target;
+    const uint32_t m = __ballot_sync(0xffffffffu, le);  // a prefix of lanes; lane 0 always
+    const uint32_t k = 31u - (uint32_t)__clz((int)m);
+    lo += k * step;
+    hi = min(hi, lo + step);
+  }
+  const uint32_t idx = lo + (uint32_t)lane;
+  const bool le = idx < hi && ptr[idx] - edge_from <= target;
+  const uint32_t m = __ballot_sync(0xffffffffu, le);
+  return lo + 31u - (uint32_t)__clz((int)m);
+}
+
 // Copies the edges of queue entries [from, from+size) from the mapped host
 // CSR to buf[0 .. edge_count).  Output positions are balanced per CTA; each
 // CTA stages the (buffer offset, host offset) of the sources its tile covers
@@ -831,29 +852,19 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(
     uint32_t edge_count) {
   __shared__ uint32_t s_bpos[kGatherTile + 1];
   __shared__ uint32_t s_hpos[kGatherTile + 1];
-  __shared__ uint32_t s_first, s_nsrc;
+  __shared__ uint32_t s_first, s_last;
   const uint32_t ntiles = (edge_count + kGatherTile - 1) / kGatherTile;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const uint32_t j0 = t * kGatherTile;
     const uint32_t j1 = min(edge_count, j0 + kGatherTile);
-    if (threadIdx.x == 0) {
-      // sources covering [j0, j1): queue indices i with ptr[i]-edge_from in range
-      uint32_t lo = from, hi = from + size;  // last i with ptr[i]-edge_from <= j0
-      while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (ptr[mid] - edge_from <= j0) lo = mid; else hi = mid;
-      }
-      uint32_t first = lo;
-      lo = first; hi = from + size;  // last i with ptr[i]-edge_from <= j1-1
-      while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (ptr[mid] - edge_from <= j1 - 1) lo = mid; else hi = mid;
-      }
-      s_first = first;
-      s_nsrc = lo - first + 1;
+    // sources covering [j0, j1): warp 0 finds the first, warp 1 the last
+    if (threadIdx.x < 64) {
+      const int lane = threadIdx.x & 31;
+      const uint32_t r = warp_last_le(ptr, from, from + size, edge_from, threadIdx.x < 32 ? j0 : j1 - 1, lane);
+      if (lane == 0) (threadIdx.x < 32 ? s_first : s_last) = r;
     }
     __syncthreads();
-    const uint32_t first = s_first, nsrc = s_nsrc;
+    const uint32_t first = s_first, nsrc = s_last - s_first + 1;
     for (uint32_t k = threadIdx.x; k < nsrc; k += blockDim.x) {
       const uint32_t i = first + k;
       s_bpos[k] = ptr[i] - edge_from;
@@ -989,30 +1000,20 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
   __shared__ uint32_t s_len[kGatherTile + 1];
   __shared__ uint32_t s_cs[kGatherTile + 1];
   __shared__ uint32_t s_part[kGatherThreads + 1];
-  __shared__ uint32_t s_first, s_nsrc;
+  __shared__ uint32_t s_first, s_last;
   const uint32_t ntiles = (edge_count + kGatherTile - 1) / kGatherTile;
   const int tid = threadIdx.x;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const uint32_t j0 = t * kGatherTile;
     const uint32_t j1 = min(edge_count, j0 + kGatherTile);
-    if (tid == 0) {
-      uint32_t lo = from, hi = from + size;
-      while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (ptr[mid] - edge_from <= j0) lo = mid; else hi = mid;
-      }
-      const uint32_t first = lo;
-      lo = first;
-      hi = from + size;
-      while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (ptr[mid] - edge_from <= j1 - 1) lo = mid; else hi = mid;
-      }
-      s_first = first;
-      s_nsrc = lo - first + 1;
+    // sources covering [j0, j1): warp 0 finds the first, warp 1 the last
+    if (tid < 64) {
+      const int lane = tid & 31;
+      const uint32_t r = warp_last_le(ptr, from, from + size, edge_from, tid < 32 ? j0 : j1 - 1, lane);
+      if (lane == 0) (tid < 32 ? s_first : s_last) = r;
     }
     __syncthreads();
-    const uint32_t first = s_first, nsrc = s_nsrc;
+    const uint32_t first = s_first, nsrc = s_last - s_first + 1;
     // per-source clipped ranges (buffer position, host record, length)
 #pragma unroll
     for (uint32_t q = 0; q < kGatherPer; ++q) {

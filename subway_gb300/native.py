@@ -24,6 +24,8 @@ OPT_NO_PACK = 0x4
 OPT_SCALAR_GATHER = 0x8
 OPT_CTA_TILES = 0x10
 OPT_SPLIT_WEIGHTS = 0x20
+OPT_BATCH_PERSISTENT = 0x40
+OPT_BATCH_GRAPH = 0x80
 SCHED_CAP_COMPACT = 0x1
 SCHED_KEEP_IDLE = 0x2
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
@@ -115,6 +117,8 @@ _PROTOS = {
     "sgw_batch_device_bytes": (C.c_int, [_P, _u64p]),
     "sgw_batch_run": (C.c_int, [_P, C.c_int, _P, C.c_uint32, _P, _P]),
     "sgw_batch_results": (C.c_int, [_P, C.POINTER(_P)]),
+    "sgw_batch_check_wait_timeout": (C.c_int, [_P, C.c_uint64]),
+    "sgw_batch_run_u16": (C.c_int, [_P, C.c_int, _P, C.c_uint32, _P, _P]),
     "sgw_range_trace_count": (C.c_int, [_P, _u64p]),
     "sgw_range_trace_read": (C.c_int, [_P, _P, C.c_uint64, _u64p]),
     "sgw_trace_enable": (C.c_int, [_P, C.c_int]),
@@ -529,20 +533,24 @@ class Batch:
         self.graph = graph
         self.lanes = lanes
 
-    def run(self, algo, sources, out=None, view=False):
+    def run(self, algo, sources, out=None, view=False, answers="u32"):
         """Distances of each query (rows).  view=True returns a read-only view of
-        the batch's pinned buffer (no copy; valid until the next run)."""
+        the batch's pinned buffer (no copy; valid until the next run).
+        answers="u16": 16-bit answers, unreached = 0xffff."""
         src = np.ascontiguousarray(sources, dtype=np.uint32)
         n = self.graph.n
+        dt = np.uint16 if answers == "u16" else np.uint32
         if out is None and not view:
-            out = np.empty((len(src), n), np.uint32)
+            out = np.empty((len(src), n), dt)
         st = BatchStats()
-        check(lib().sgw_batch_run(self.h, ALGOS.get(algo, algo), _ptr(src), len(src),
-                                  _ptr(out) if out is not None else None, C.byref(st)), "sgw_batch_run")
+        fn = lib().sgw_batch_run_u16 if answers == "u16" else lib().sgw_batch_run
+        check(fn(self.h, ALGOS.get(algo, algo), _ptr(src), len(src), _ptr(out) if out is not None else None,
+                 C.byref(st)), "sgw_batch_run")
         if out is None:
             p = _P()
             check(lib().sgw_batch_results(self.h, C.byref(p)), "sgw_batch_results")
-            out = np.ctypeslib.as_array(C.cast(p, _u32p), shape=(len(src), n))
+            ptr_t = C.POINTER(C.c_uint16) if answers == "u16" else _u32p
+            out = np.ctypeslib.as_array(C.cast(p, ptr_t), shape=(len(src), n))
             out.flags.writeable = False
         return out, {k: getattr(st, k) for k, _ in st._fields_ if k != "reserved"}
 
@@ -550,6 +558,10 @@ class Batch:
         v = C.c_uint64()
         check(lib().sgw_batch_device_bytes(self.h, C.byref(v)), "sgw_batch_device_bytes")
         return v.value
+
+    def check_wait_timeout(self, wait_ns=2_000_000) -> int:
+        """Status of one persistent run whose grid barriers cannot fill (SGW_ETIMEOUT expected)."""
+        return lib().sgw_batch_check_wait_timeout(self.h, int(wait_ns))
 
     def close(self):
         if self.h and self.h.value:

@@ -29,7 +29,7 @@ import numpy as np
 from . import native as N
 
 
-def admit(graphs, lanes, budget_bytes, device=0, chunk_edges=0):
+def admit(graphs, lanes, budget_bytes, device=0, chunk_edges=0, flags=0):
     """Batch objects for the graphs that fit the remaining budget, in order.
     chunk_edges: one value for all graphs or one per graph (0 = default)."""
     left = budget_bytes
@@ -37,7 +37,7 @@ def admit(graphs, lanes, budget_bytes, device=0, chunk_edges=0):
     chunks = chunk_edges if isinstance(chunk_edges, (list, tuple)) else [chunk_edges] * len(graphs)
     for g, ch in zip(graphs, chunks):
         try:
-            b = N.Batch(g, lanes=lanes, budget_bytes=left, device=device, chunk_edges=ch)
+            b = N.Batch(g, lanes=lanes, budget_bytes=left, device=device, chunk_edges=ch, flags=flags)
         except N.SgwError as e:
             if e.status != -5:  # only a budget refusal means "not admitted"
                 raise
@@ -62,7 +62,7 @@ def shard(stream, world=1, rank=0):
     return tuple(x[rank::world] for x in stream)
 
 
-def serve_stream(batches, arrivals, target, sources, algo="bfs", lanes=64):
+def serve_stream(batches, arrivals, target, sources, algo="bfs", lanes=64, answers="u32"):
     """Serves one stream in real time; returns answer times (s from the
     start of the clock) and the batch sizes."""
     queries = len(arrivals)
@@ -85,7 +85,7 @@ def serve_stream(batches, arrivals, target, sources, algo="bfs", lanes=64):
         k = min((i for i in range(len(batches)) if pending[i]), key=lambda i: arrivals[pending[i][0]])
         ids = pending[k][:lanes]
         pending[k] = pending[k][lanes:]
-        batches[k].run(algo, sources[ids], view=True)  # answers land in pinned memory
+        batches[k].run(algo, sources[ids], view=True, answers=answers)  # answers land in pinned memory
         t = time.perf_counter() - t0
         done[ids] = t
         served += len(ids)
@@ -102,19 +102,19 @@ def summarize(arrivals, done, sizes, rate, algo):
             "mean_batch": float(np.mean(sizes)), "max_batch": int(max(sizes))}
 
 
-def serve(batches, algo="bfs", queries=4096, rate=2000.0, seed=5, lanes=64):
+def serve(batches, algo="bfs", queries=4096, rate=2000.0, seed=5, lanes=64, answers="u32"):
     arrivals, target, sources = make_stream([b.graph.n for b in batches], queries, rate, seed)
-    done, sizes = serve_stream(batches, arrivals, target, sources, algo, lanes)
+    done, sizes = serve_stream(batches, arrivals, target, sources, algo, lanes, answers)
     return summarize(arrivals, done, sizes, rate, algo)
 
 
-def serve_replicas(batches, pg, algo="bfs", queries=4096, rate=2000.0, seed=5, lanes=64):
+def serve_replicas(batches, pg, algo="bfs", queries=4096, rate=2000.0, seed=5, lanes=64, answers="u32"):
     """One replica's share of the stream; rank 0 returns the merged summary,
     the other ranks None.  pg: torch.distributed, initialised."""
     world, rank = pg.get_world_size(), pg.get_rank()
     arrivals, target, sources = shard(make_stream([b.graph.n for b in batches], queries, rate, seed), world, rank)
     pg.barrier()
-    done, sizes = serve_stream(batches, arrivals, target, sources, algo, lanes)
+    done, sizes = serve_stream(batches, arrivals, target, sources, algo, lanes, answers)
     parts = [None] * world
     pg.all_gather_object(parts, (arrivals, done, sizes))
     if rank != 0:
@@ -136,6 +136,10 @@ def main():
     ap.add_argument("--budget", type=float, default=200e9)
     ap.add_argument("--chunk-edges", type=int, default=0)
     ap.add_argument("--autotune", action="store_true", help="pick each graph's edges per work item by timing")
+    ap.add_argument("--answers", default="u32", choices=["u32", "u16"],
+                    help="u16: 16-bit answers (unreached = 0xffff), half the bytes copied out")
+    ap.add_argument("--form", default="auto", choices=["auto", "persistent", "graph"],
+                    help="batch form: auto (persistent for SSSP, graph loop for BFS), or one for both")
     a = ap.parse_args()
     import os
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -153,21 +157,23 @@ def main():
         from .autotune import tune_batch
         tuned = [tune_batch(g, a.algo, a.lanes, device=device) for g in graphs]
         chunks = [best for best, _ in tuned]
-    admitted, rejected = admit(graphs, a.lanes, int(a.budget), device=device, chunk_edges=chunks)
+    admitted, rejected = admit(graphs, a.lanes, int(a.budget), device=device, chunk_edges=chunks,
+                               flags={"auto": 0, "persistent": N.OPT_BATCH_PERSISTENT,
+                                      "graph": N.OPT_BATCH_GRAPH}[a.form])
     # warm the graphs up once
     for b in admitted:
         b.run(a.algo, np.zeros(1, np.uint32))
     if pg:
-        res = serve_replicas(admitted, pg, a.algo, a.queries, a.rate, lanes=a.lanes)
+        res = serve_replicas(admitted, pg, a.algo, a.queries, a.rate, lanes=a.lanes, answers=a.answers)
         if res is None:
             pg.destroy_process_group()
             return
     else:
-        res = serve(admitted, a.algo, a.queries, a.rate, lanes=a.lanes)
+        res = serve(admitted, a.algo, a.queries, a.rate, lanes=a.lanes, answers=a.answers)
     if tuned:
         res["autotune"] = [{"scale": s, "chunk_edges": best, "trials_ms": [(c, round(ms, 2)) for c, ms in trials]}
                            for s, (best, trials) in zip(a.scales, tuned)]
-    res.update({"scales_admitted": [s for s, g in zip(a.scales, graphs) if g not in rejected],
+    res.update({"answers": a.answers, "form": a.form, "scales_admitted": [s for s, g in zip(a.scales, graphs) if g not in rejected],
                 "device_bytes": sum(b.device_bytes() for b in admitted), "generate_s": round(t_gen, 1)})
     print(json.dumps(res))
     if pg:

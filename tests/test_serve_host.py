@@ -25,7 +25,7 @@ class _FakeBatch:
         self.graph = _G(n)
         self.log = log if log is not None else []
 
-    def run(self, algo, sources, view=False):
+    def run(self, algo, sources, view=False, answers="u32"):
         self.log.append(np.asarray(sources).copy())
         time.sleep(0.0005)
 
