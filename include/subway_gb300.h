@@ -75,7 +75,11 @@ int sgw_graph_load(const char *path, sgw_graph **out);
  * pointers are copied (plus the sentinel node_pointer[n] = m, which the file
  * does not hold).  The file is validated like sgw_graph_load (size, monotone
  * pointers, endpoints < n), which reads every record once.  The mapping is
- * released by sgw_graph_free; the file must not be truncated meanwhile.
+ * released by sgw_graph_free.  Until then the file must not change: the
+ * mapping is shared, so a process that truncates or rewrites it (the
+ * converter writing to the same path, say) makes later reads fault (SIGBUS)
+ * or see edges that were never validated; write a new file and rename it
+ * over the old one instead, which leaves the mapped copy intact.
  * A .bwcsr file with an odd vertex count is read as by sgw_graph_load
  * instead, since its 8-byte records would not be 8-byte aligned. */
 int sgw_graph_map(const char *path, sgw_graph **out);

@@ -131,10 +131,15 @@ def test_learned_policy_uses_residency(gpu):
 
 def test_trained_network_gains(gpu):
     """What the trained network adds, on a graph it was not trained on
-    (R-MAT scale 20, seed 777; training used scales 22-25): it predicts the
-    next iteration's range activity better than assuming the activity stays
-    the same, and the learned policy built on it relaxes far fewer edges than
-    the plain policy while moving no more bytes, with identical answers."""
+    (R-MAT scale 20, seed 777; training used scales 22-25), measured against
+    the same schedule with the persistence predictor ("the active fraction
+    stays the same") in place of the network: the network predicts the next
+    iteration's range activity better, the answers are identical, and the
+    schedule's cost (H2D bytes, relaxed edges) stays within 10% of the
+    persistence predictor's.  On these workloads the schedule's decisions
+    are not sensitive to the prediction error, so the network buys no
+    measurable time or bytes (the design notes give the measurements); both
+    learned schedules still relax far fewer edges than the plain one."""
     from subway_gb300 import scheduler
     model = scheduler.load_default(0)
     assert model is not None, "trained scheduler model missing"
@@ -147,16 +152,19 @@ def test_trained_network_gains(gpu):
 
     budget = int(scheduler.fixed_state_bytes(g.n) + 0.4 * g.m * 4)
     plain = gpu.Engine(g, budget_bytes=budget)
-    learned = gpu.Engine(g, budget_bytes=budget, num_buffers=3)
-    learned.set_policy("learned", model)
-    tot = {"plain": [0, 0], "learned": [0, 0]}
+    net = gpu.Engine(g, budget_bytes=budget, num_buffers=3)
+    net.set_policy("learned", model)
+    same = gpu.Engine(g, budget_bytes=budget, num_buffers=3)
+    same.set_policy("learned", None)
+    tot = {k: [0, 0] for k in ("plain", "net", "same")}
     for s in g.pick_sources(3, seed=9):
-        v1, s1 = plain.run("sssp", "async", int(s))
-        v2, s2 = learned.run("sssp", "async", int(s))
-        assert np.array_equal(v1, v2)
-        tot["plain"][0] += s1["h2d_bytes"]
-        tot["plain"][1] += s1["relaxed_edges"]
-        tot["learned"][0] += s2["h2d_bytes"]
-        tot["learned"][1] += s2["relaxed_edges"]
-    assert tot["learned"][0] <= tot["plain"][0], tot
-    assert tot["learned"][1] < 0.9 * tot["plain"][1], tot
+        ref = None
+        for k, eng in (("plain", plain), ("net", net), ("same", same)):
+            v, st = eng.run("sssp", "async", int(s))
+            ref = v if ref is None else ref
+            assert np.array_equal(v, ref), k
+            tot[k][0] += st["h2d_bytes"]
+            tot[k][1] += st["relaxed_edges"]
+    assert tot["net"][0] <= 1.1 * tot["same"][0] and tot["net"][1] <= 1.1 * tot["same"][1], tot
+    assert tot["net"][0] <= tot["plain"][0], tot
+    assert tot["net"][1] < 0.9 * tot["plain"][1], tot
