@@ -1322,8 +1322,13 @@ __global__ void __launch_bounds__(kRelaxThreads) k_relax_tile(RelaxArgs a) {
 // leave publishes them.  Sources above tile_degree_max go to the chunk list
 // as in the CTA form.
 constexpr int kWarpsPerCta = kRelaxThreads / 32;
+// Resident CTAs per SM the warp relaxation is compiled for (registers are
+// capped to fit them); 4 keeps it free of spills.
+#ifndef SGW_RELAX_MIN_BLOCKS
+#define SGW_RELAX_MIN_BLOCKS 4
+#endif
 template <int ALGO, bool ASYNC, int W>
-__global__ void __launch_bounds__(kRelaxThreads, 4) k_relax_warp(RelaxArgs a) {
+__global__ void __launch_bounds__(kRelaxThreads, SGW_RELAX_MIN_BLOCKS) k_relax_warp(RelaxArgs a) {
   __shared__ int s_skip;
   __shared__ unsigned long long s_edges, s_srcs;
   __shared__ uint32_t s_any, s_done;
