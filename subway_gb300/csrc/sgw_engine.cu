@@ -543,12 +543,13 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
   CK(cudaStreamWaitEvent(s, e->ev_free[b], 0));
   size_t slot = 0;
   TRY(prof_begin(e, K_GATHER, s, &slot));
-  // default grid: 2 CTAs per SM for the plain schedule's full partitions, 3
-  // per 2 SMs for the learned schedule (measured best on RMAT-24 / 1 GB and
-  // RMAT-28 / 8 GB: fewer gather CTAs leave the concurrent relaxation more of
-  // each SM's registers; with one per SM the gather no longer keeps up)
-  const uint32_t gdef = e->policy == SGW_POLICY_LEARNED ? (3u * e->num_sms + 1u) / 2u : 2u * e->num_sms;
-  const uint32_t gmax = e->opts.gather_ctas ? e->opts.gather_ctas : gdef;
+  // default grid: 2 CTAs per SM (measured on RMAT-28 / 8 GB, learned
+  // schedule, one process, alternating order: 163.9 ms per run against 167.6
+  // with 1.5 per SM and 166.3 with 3; within 1.5% at RMAT-24 / 1 GB).  Fewer
+  // gather CTAs leave the concurrent relaxation more of each SM (72 against
+  // 116 ms of relaxation per run at 1.5 and 3 per SM); with one per SM the
+  // gather no longer keeps up with the host link.
+  const uint32_t gmax = e->opts.gather_ctas ? e->opts.gather_ctas : 2u * e->num_sms;
   const uint32_t grid = std::min<uint32_t>(grid_for(e, q.edge_count, kGatherTile), gmax);
   const uint4 *h16 = reinterpret_cast<const uint4 *>(e->d_host_edges);
   if (e->vec_gather && e->W == 1 && e->use_w)  // split form: destination words and weight bytes
