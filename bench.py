@@ -272,7 +272,54 @@ def run_ours(a, dist):
         return e
 
     arms = {"plain": ["plain"], "learned": ["learned"], "all": ["plain", "rules", "learned"]}[a.policy]
-    res, engines = {}, {}
+
+    # the oracle's answers first (the CPU baseline, timed with the GPU idle);
+    # every schedule is checked against them right after its timed loop, so
+    # one engine at a time holds its pinned transfer copy
+    check = {"checked_sources": 0, "mismatches": 0, "reached_mismatches": 0}
+    cpu, refs = None, {}
+    if a.check == "all":
+        from oracle import oracle
+        e = g.edges if weighted else g.ends
+        deg = g.out_degree()
+        secs, reached_cpu = 0.0, 0
+        for s in dict.fromkeys(sources):
+            t = time.perf_counter()
+            ref = oracle.run(a.algo, g.node_pointer, e, s, parallel=True)
+            secs += time.perf_counter() - t
+            want = int(deg[ref != (0 if a.algo == "sswp" else INF)].astype(np.uint64).sum())
+            reached_cpu += want
+            refs[s] = (ref, want)
+        check["checked_sources"] = len(refs)
+        cpu = {"value": round(reached_cpu / secs / 1e9, 4), "unit": "GTEPS", "cores": oracle.num_threads(),
+               "kind": "port",
+               "sample": f"{len(refs)} full {a.algo} runs of the OpenMP oracle "
+                         f"({'delta-stepping' if a.algo == 'sssp' else 'frontier label-correcting'}) on the "
+                         "same graph, the runs that check the engine's answers",
+               "seconds": round(secs, 2)}
+
+    def check_engine(arm, eng):
+        for s, (ref, want) in refs.items():
+            _, st = eng.run(a.algo, a.mode, s, out=out)
+            check["mismatches"] += int(np.count_nonzero(out != ref))
+            check["reached_mismatches"] += int(st["reached_edges"] != want)
+        # where tests/golden holds the reference build's own digests for this
+        # workload, the learned schedule's distances are compared with them too
+        import hashlib
+        gold = ROOT / "tests" / "golden" / f"ref_rmat{a.scale}_{a.algo}_{a.mode}_{int(a.budget / 1e9)}gb.json"
+        if arm == "learned" and a.check == "all" and gold.exists() and a.edge_factor == 16:
+            rep = json.loads(gold.read_text())
+            if f"seed {a.seed}," in rep["graph"] and rep["budget_bytes"] == int(a.budget):
+                hits = 0
+                for s in rep["sources"]:
+                    eng.run(a.algo, a.mode, s, out=out)
+                    key = next(k for k in rep["runs"] if k.startswith("fixed/") and k.endswith(f"/s{s}"))
+                    hits += hashlib.sha256(out.tobytes()).hexdigest() == rep["runs"][key]["sha256"]
+                check["reference_digests"] = {"checked": len(rep["sources"]), "equal": hits,
+                                              "fixture": gold.name}
+                check["mismatches"] += len(rep["sources"]) - hits
+
+    res = {}
     for arm in arms:
         t = time.perf_counter()
         eng = make_engine(arm)
@@ -291,7 +338,6 @@ def run_ours(a, dist):
             t_total = time.perf_counter() - t_start
         dist.barrier()
         res[arm] = {"steps": steps, "clk": clk, "t_total": t_total, "create_s": create_s}
-        engines[arm] = eng
         if arm == "learned":
             # one more run, untimed, with the range trace on: how often the
             # predictions behind its transfer decisions were wrong
@@ -299,6 +345,9 @@ def run_ours(a, dist):
             eng.run(a.algo, a.mode, sources[0], out=out)
             res[arm]["mispredicted"] = scheduler.mispredictions(eng.range_trace())
             eng.trace_enable(False)
+        check_engine(arm, eng)
+        eng.close()
+        del eng
 
     # one query as a process runs it: create, run with host buffers, destroy
     for arm in [x for x in ("plain", "learned") if x in arms]:
@@ -314,49 +363,7 @@ def run_ours(a, dist):
                 st_all.append(st)
         res[arm]["e2e_walls"] = walls
         res[arm]["e2e_reached"] = sum(s["reached_edges"] for s in st_all)
-
-    # parity: every distinct source, every schedule, against the oracle
-    check = {"checked_sources": 0, "mismatches": 0, "reached_mismatches": 0}
-    cpu = None
-    if a.check == "all":
-        from oracle import oracle
-        e = g.edges if weighted else g.ends
-        deg = g.out_degree()
-        secs, reached_cpu = 0.0, 0
-        for s in dict.fromkeys(sources):
-            t = time.perf_counter()
-            ref = oracle.run(a.algo, g.node_pointer, e, s, parallel=True)
-            secs += time.perf_counter() - t
-            want = int(deg[ref != (0 if a.algo == "sswp" else INF)].astype(np.uint64).sum())
-            reached_cpu += want
-            for arm, eng in engines.items():
-                _, st = eng.run(a.algo, a.mode, s, out=out)
-                check["mismatches"] += int(np.count_nonzero(out != ref))
-                check["reached_mismatches"] += int(st["reached_edges"] != want)
-            check["checked_sources"] += 1
-        # where tests/golden holds the reference build's own digests for this
-        # workload, the learned schedule's distances are compared with them too
-        import hashlib
-        gold = ROOT / "tests" / "golden" / f"ref_rmat{a.scale}_{a.algo}_{a.mode}_{int(a.budget / 1e9)}gb.json"
-        if "learned" in engines and gold.exists() and a.edge_factor == 16:
-            rep = json.loads(gold.read_text())
-            if f"seed {a.seed}," in rep["graph"] and rep["budget_bytes"] == int(a.budget):
-                hits = 0
-                for s in rep["sources"]:
-                    engines["learned"].run(a.algo, a.mode, s, out=out)
-                    key = next(k for k in rep["runs"] if k.startswith("fixed/") and k.endswith(f"/s{s}"))
-                    hits += hashlib.sha256(out.tobytes()).hexdigest() == rep["runs"][key]["sha256"]
-                check["reference_digests"] = {"checked": len(rep["sources"]), "equal": hits,
-                                              "fixture": gold.name}
-                check["mismatches"] += len(rep["sources"]) - hits
-        cpu = {"value": round(reached_cpu / secs / 1e9, 4), "unit": "GTEPS", "cores": oracle.num_threads(),
-               "kind": "port",
-               "sample": f"{check['checked_sources']} full {a.algo} runs of the OpenMP oracle "
-                         f"({'delta-stepping' if a.algo == 'sssp' else 'frontier label-correcting'}) on the "
-                         "same graph, the runs that check the engine's answers",
-               "seconds": round(secs, 2)}
-    for eng in engines.values():
-        eng.close()
+    refs.clear()
 
     hbm_peak, hbm_src = measured_peaks()
 

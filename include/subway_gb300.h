@@ -169,7 +169,11 @@ typedef struct sgw_engine_opts {
    * whole frontier.  Under this policy active vertices that cannot push
    * (value INF for BFS/SSSP, 0 for SSWP) are never transferred. */
   uint32_t sched_defer_permille;
-  uint32_t reserved[2];
+  /* The host transfer copy is allocated in pinned chunks of
+   * 2^transfer_chunk_log2 bytes (0 = 30, i.e. 1 GiB; at most 64 chunks per
+   * stream, larger chunks if needed), two chunks at a time. */
+  uint32_t transfer_chunk_log2;
+  uint32_t reserved;
 } sgw_engine_opts;
 
 void sgw_engine_opts_default(sgw_engine_opts *opts);

@@ -10,6 +10,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <memory>
+#include <thread>
 #include <vector>
 
 #include "sgw_internal.h"
@@ -41,6 +44,18 @@ struct ProfEvent {
 };
 
 constexpr int kMaxBuf = 8;  // edge buffers an engine can hold
+constexpr int kMaxHostChunks = 64;  // pieces of one host transfer stream
+
+// One stream of the host transfer copy (edge words, or the split form's
+// weight bytes) in pinned, mapped chunks of 2^shift bytes; 16 zero bytes
+// follow the data in the last chunk for the gather's vector reads.
+struct HostStream {
+  std::vector<char *> h;               // host addresses of the chunks
+  std::vector<size_t> size;            // allocated bytes of each chunk
+  std::vector<unsigned long long> d;   // device addresses of the chunks
+  uint32_t shift = 30;
+  size_t bytes = 0;                    // data bytes
+};
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -84,8 +99,9 @@ struct sgw_engine {
   // host side
   Ctl *h_ctl = nullptr;
   Part *h_parts = nullptr;
-  const uint32_t *d_host_edges = nullptr;  // device view of the transfer records
-  const void *h_src = nullptr;             // host view of the transfer records
+  HostStream hs_ends;                      // transfer records (destination words)
+  HostStream hs_w;                         // split form: weight bytes
+  unsigned long long *d_hct = nullptr;     // device chunk tables: ends, then weights
   // Split form: weights below 256 that do not pack beside the vertex id
   // travel as a separate byte stream (5 bytes per edge instead of 8).
   double dma_gbs = -1.0;                   // measured DMA rate from the transfer copy (-1: not timed)
@@ -93,12 +109,9 @@ struct sgw_engine {
   double stream_ms = 0.0;
   bool split = false;
   bool use_w = false;                      // this run reads the weight stream
-  const uint4 *d_host_w16 = nullptr;       // device view of the weight stream
-  const char *h_wsrc = nullptr;            // host view of the weight stream
   uint8_t *d_wbuf[kMaxBuf] = {};           // weight bytes of each edge buffer
   uint32_t rec_bytes = 4;                  // device bytes per edge in a buffer
-  uint32_t *h_packed = nullptr;            // packed transfer copy (weighted graphs)
-  size_t packed_bytes = 0;
+  size_t packed_bytes = 0;                 // bytes of the whole transfer copy
 
   bool vec_gather = false;                 // host records readable as aligned 16-B words
   uint32_t cur_streamed = 0;               // partition being relaxed: whole-range buffer
@@ -192,6 +205,106 @@ int check_ctl_error(sgw_engine *e) {
   return fail(SGW_ECUDA, "device error code %u", err);
 }
 
+// DMA copy of bytes [off, off + bytes) of a host stream, one cudaMemcpyAsync
+// per chunk it touches.
+int copy_from_host(const HostStream &hs, void *dst, size_t off, size_t bytes, cudaStream_t st) {
+  char *d = static_cast<char *>(dst);
+  const size_t cb = size_t(1) << hs.shift;
+  while (bytes) {
+    const size_t k = off >> hs.shift, o = off & (cb - 1);
+    const size_t n = std::min(bytes, cb - o);
+    CK(cudaMemcpyAsync(d, hs.h[k] + o, n, cudaMemcpyHostToDevice, st));
+    d += n;
+    off += n;
+    bytes -= n;
+  }
+  return SGW_OK;
+}
+
+// Chunk sizes of a stream of `bytes` data bytes: chunks of 2^log2_chunk bytes
+// (1 GiB by default, at least 4 KiB; larger powers of two when more than
+// kMaxHostChunks would be needed), the last one cut to what remains plus 16
+// zero bytes, all multiples of 16.
+void plan_stream(HostStream &hs, size_t bytes, uint32_t log2_chunk) {
+  hs.bytes = bytes;
+  hs.shift = log2_chunk ? std::max<uint32_t>(log2_chunk, 12u) : 30u;
+  const size_t total = bytes + 16;
+  while (((total + (size_t(1) << hs.shift) - 1) >> hs.shift) > (size_t)kMaxHostChunks) ++hs.shift;
+  const size_t cb = size_t(1) << hs.shift, k = (total + cb - 1) / cb;
+  hs.h.assign(k, nullptr);
+  hs.d.assign(k, 0);
+  hs.size.assign(k, cb);
+  hs.size[k - 1] = (total - (k - 1) * cb + 15) / 16 * 16;
+}
+
+// Allocates the chunks of both streams with two host threads while the
+// calling thread fills each chunk as soon as it exists (fill(stream, k)):
+// pinned allocation is mostly the driver zeroing and locking pages, and two
+// calls in flight at once take about 0.6 of the time one call takes for the
+// same bytes (21 GiB on a GB300 host: 0.78 s against 1.27 s; more threads
+// did not help), while filling a chunk takes all host cores for a fraction
+// of its allocation time.
+template <class Fill>
+cudaError_t alloc_and_fill(HostStream &a, HostStream &b, Fill fill) {
+  std::vector<std::pair<HostStream *, size_t>> items;
+  for (size_t i = 0; i < a.h.size(); ++i) items.push_back({&a, i});
+  for (size_t i = 0; i < b.h.size(); ++i) items.push_back({&b, i});
+  std::unique_ptr<std::atomic<int>[]> state(new std::atomic<int>[items.size()]);  // 0 pending, 1 ready, 2 failed
+  for (size_t i = 0; i < items.size(); ++i) state[i].store(0);
+  std::atomic<int> stop{0};
+  cudaError_t err[2] = {cudaSuccess, cudaSuccess};
+  auto work = [&](int t) {
+    for (size_t i = (size_t)t; i < items.size(); i += 2) {
+      if (stop.load()) { state[i].store(2); continue; }
+      HostStream &hs = *items[i].first;
+      const size_t k = items[i].second;
+      void *p = nullptr;
+      const cudaError_t ce = cudaHostAlloc(&p, hs.size[k], cudaHostAllocMapped | cudaHostAllocPortable);
+      if (ce != cudaSuccess) {
+        err[t] = ce;
+        stop.store(1);
+        state[i].store(2);
+        continue;
+      }
+      hs.h[k] = static_cast<char *>(p);
+      state[i].store(1);
+    }
+  };
+  std::thread t0(work, 0), t1(work, 1);
+  for (size_t i = 0; i < items.size(); ++i) {
+    int st;
+    while ((st = state[i].load()) == 0) std::this_thread::yield();
+    if (st != 1) break;
+    fill(*items[i].first, items[i].second);
+  }
+  t0.join();
+  t1.join();
+  return err[0] != cudaSuccess ? err[0] : err[1];
+}
+
+// Frees both streams' chunks, two at a time (as they were allocated).
+void free_streams(HostStream &a, HostStream &b) {
+  std::vector<char *> all;
+  for (char *p : a.h) if (p) all.push_back(p);
+  for (char *p : b.h) if (p) all.push_back(p);
+  auto work = [&](size_t t) {
+    for (size_t i = t; i < all.size(); i += 2) cudaFreeHost(all[i]);
+  };
+  if (all.size() > 1) {
+    std::thread other(work, 1);
+    work(0);
+    other.join();
+  } else {
+    work(0);
+    work(1);
+  }
+  for (HostStream *hs : {&a, &b}) {
+    hs->h.clear();
+    hs->d.clear();
+    hs->size.clear();
+  }
+}
+
 // Whole-range streaming moves records by DMA from the transfer copy.  On
 // some GB300 machines the learned policy's transfers ran at half their
 // usual rate while the plain policy's gathers did not, so the engine times a
@@ -201,9 +314,10 @@ int check_ctl_error(sgw_engine *e) {
 // to time: the rate is then taken as good.
 int probe_stream_dma(sgw_engine *e) {
   e->dma_gbs = -1.0;
-  const size_t bytes = std::min<size_t>(std::min<size_t>(e->packed_bytes, (size_t)e->cap * 4 * e->W),
+  if (e->hs_ends.h.empty()) return SGW_OK;
+  const size_t bytes = std::min<size_t>(std::min<size_t>(e->hs_ends.size[0], (size_t)e->cap * 4 * e->W),
                                         size_t(256) << 20) & ~size_t(15);
-  if (!e->h_packed || bytes < (size_t(64) << 20)) return SGW_OK;
+  if (bytes < (size_t(64) << 20)) return SGW_OK;
   cudaEvent_t a = nullptr, b = nullptr;
   CK(cudaEventCreate(&a));
   if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return fail(SGW_ECUDA, "event creation"); }
@@ -211,7 +325,7 @@ int probe_stream_dma(sgw_engine *e) {
   int st = SGW_OK;
   for (int i = 0; i < 4 && st == SGW_OK; ++i) {  // the first copy warms up
     cudaEventRecord(a, e->s_copy);
-    cudaMemcpyAsync(e->d_buf[0], e->h_packed, bytes, cudaMemcpyHostToDevice, e->s_copy);
+    cudaMemcpyAsync(e->d_buf[0], e->hs_ends.h[0], bytes, cudaMemcpyHostToDevice, e->s_copy);
     cudaEventRecord(b, e->s_copy);
     if (cudaEventSynchronize(b) != cudaSuccess) { st = fail(SGW_ECUDA, "transfer-copy DMA probe"); break; }
     float ms = 0;
@@ -242,7 +356,7 @@ int read_ctl(sgw_engine *e) {
 enum Family { FAM_INT = 0, FAM_PR = 1 };
 
 struct Layout {
-  size_t off, tflag, tagg, tincl, ctl, mlp, sel, gmask;  // common
+  size_t off, tflag, tagg, tincl, ctl, mlp, sel, gmask, hct;  // common
   size_t value, l1, l2, queue, ptr, delta, qpush;     // family
   size_t parts, ranges, rstat, wl, buf[kMaxBuf], total;
   uint64_t cap;
@@ -262,6 +376,7 @@ Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
   L.mlp = take(sizeof(__nv_bfloat16) * kMlpParams);
   L.sel = take(sizeof(unsigned long long) * kSelBins);
   L.gmask = take(4ull * ((n + kGenVPerLane - 1) / kGenVPerLane));
+  L.hct = take(2ull * kMaxHostChunks * sizeof(unsigned long long));
   if (fam == FAM_INT) {
     L.value = take(4ull * n);
     L.l1 = take(n);
@@ -322,6 +437,7 @@ int carve(sgw_engine *e, int fam, uint64_t cap) {
   e->d_tincl = (unsigned long long *)(b + L.tincl);
   e->d_ctl = (Ctl *)(b + L.ctl);
   e->d_gmask = (uint32_t *)(b + L.gmask);
+  e->d_hct = (unsigned long long *)(b + L.hct);
   e->d_value = (uint32_t *)(b + L.value);
   e->d_l1 = fam == FAM_INT ? (uint8_t *)(b + L.l1) : nullptr;
   e->d_l2 = fam == FAM_INT ? (uint8_t *)(b + L.l2) : nullptr;
@@ -551,27 +667,26 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
   // gather no longer keeps up with the host link.
   const uint32_t gmax = e->opts.gather_ctas ? e->opts.gather_ctas : 2u * e->num_sms;
   const uint32_t grid = std::min<uint32_t>(grid_for(e, q.edge_count, kGatherTile), gmax);
-  const uint4 *h16 = reinterpret_cast<const uint4 *>(e->d_host_edges);
+  const HostChunks h16{e->d_hct, e->hs_ends.shift};
+  const HostChunks hw16{e->d_hct + kMaxHostChunks, e->hs_w.shift};
   if (e->vec_gather && e->W == 1 && e->use_w)  // split form: destination words and weight bytes
     k_gather_v<4, true><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
-                                                        e->d_host_w16, e->d_wbuf[b], q.from, q.size,
+                                                        hw16, e->d_wbuf[b], q.from, q.size,
                                                         q.edge_from, (uint32_t)q.edge_count);
   else if (e->vec_gather && e->W == 1)
     k_gather_v<4, false><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
-                                                         nullptr, nullptr, q.from, q.size, q.edge_from,
+                                                         hw16, nullptr, q.from, q.size, q.edge_from,
                                                          (uint32_t)q.edge_count);
   else if (e->vec_gather)
     k_gather_v<8, false><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
-                                                         nullptr, nullptr, q.from, q.size, q.edge_from,
+                                                         hw16, nullptr, q.from, q.size, q.edge_from,
                                                          (uint32_t)q.edge_count);
   else if (e->W == 1)
-    k_gather<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_edges,
-                                                e->d_buf[b], q.from, q.size, q.edge_from,
-                                                (uint32_t)q.edge_count);
+    k_gather<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b], q.from,
+                                                q.size, q.edge_from, (uint32_t)q.edge_count);
   else
-    k_gather<2><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, e->d_host_edges,
-                                                e->d_buf[b], q.from, q.size, q.edge_from,
-                                                (uint32_t)q.edge_count);
+    k_gather<2><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b], q.from,
+                                                q.size, q.edge_from, (uint32_t)q.edge_count);
   CK(cudaGetLastError());
   e->stats.h2d_bytes += q.edge_count * (4ull * e->W + (e->use_w ? 1 : 0));
   e->stats.gather_bytes += q.edge_count * (4ull * e->W + (e->use_w ? 1 : 0));
@@ -709,12 +824,11 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
     const uint32_t cnt = (uint32_t)std::min<uint64_t>(e->cap, deg - s);
     size_t slot = 0;
     TRY(prof_begin(e, K_STREAM, e->s_comp, &slot));
-    CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->h_src + (hoff + s) * esz, cnt * esz,
-                       cudaMemcpyHostToDevice, e->s_comp));
+    TRY(copy_from_host(e->hs_ends, e->d_buf[b], (hoff + s) * esz, cnt * esz, e->s_comp));
     e->stats.h2d_bytes += cnt * esz;
     e->stream_bytes += cnt * esz + (e->use_w ? cnt : 0);
     if (e->use_w) {
-      CK(cudaMemcpyAsync(e->d_wbuf[b], e->h_wsrc + hoff + s, cnt, cudaMemcpyHostToDevice, e->s_comp));
+      TRY(copy_from_host(e->hs_w, e->d_wbuf[b], hoff + s, cnt, e->s_comp));
       e->stats.h2d_bytes += cnt;
     }
     TRY(prof_end(e, e->s_comp, slot));
@@ -924,11 +1038,9 @@ int range_transfer(sgw_engine *e, Job &j, int b) {
     e->stream_bytes += bytes + (e->use_w ? (size_t)(r.e1 - r.e0) : 0);
     // a whole range is contiguous: one DMA copy, no SM time taken from the
     // relaxation running on the compute stream
-    CK(cudaMemcpyAsync(e->d_buf[b], (const char *)e->h_src + (size_t)r.e0 * esz, bytes,
-                       cudaMemcpyHostToDevice, e->s_copy));
+    TRY(copy_from_host(e->hs_ends, e->d_buf[b], (size_t)r.e0 * esz, bytes, e->s_copy));
     if (e->use_w) {
-      CK(cudaMemcpyAsync(e->d_wbuf[b], e->h_wsrc + r.e0, (size_t)(r.e1 - r.e0), cudaMemcpyHostToDevice,
-                         e->s_copy));
+      TRY(copy_from_host(e->hs_w, e->d_wbuf[b], r.e0, (size_t)(r.e1 - r.e0), e->s_copy));
       e->stats.h2d_bytes += (size_t)(r.e1 - r.e0);
     }
     TRY(prof_end(e, e->s_copy, slot));
@@ -1296,41 +1408,60 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   auto cleanup = [&](int s) { sgw_engine_destroy(e); return s; };
   // The transfer copy: the edge records (packed when they fit) in pinned,
   // mapped host memory from cudaHostAlloc, read in place by the gather
-  // kernels and by DMA copies.  Ordinary pages written by all host threads
-  // and then registered with cudaHostRegister cost less to set up (0.5 s
-  // against 1.2 s for the 21 GB copy of RMAT-28 on a GB300 host), but the GPU
-  // then reached them through host page-table translations: the plain
-  // schedule's gathers, which touch rows all over the copy, ran at 7-9 GB/s
-  // instead of 130-170 GB/s.  16 bytes of padding let the 16-byte vector
-  // reads run past the last record.
+  // kernels and by DMA copies, in chunks (HostStream) so that two host
+  // threads can allocate it at once.  Ordinary pages written by all host
+  // threads and then registered with cudaHostRegister cost less to set up
+  // (0.5 s against 1.2 s for the 21 GB copy of RMAT-28 on a GB300 host), but
+  // the GPU then reached them through host page-table translations: the
+  // plain schedule's gathers, which touch rows all over the copy, ran at 7-9
+  // GB/s instead of 130-170 GB/s.
   if (g->m > 0) {
-    const size_t rec_bytes = (size_t)e->m * 4 * e->W;
-    const size_t ends_alloc = (rec_bytes + 16 + 15) / 16 * 16;
-    const size_t w_alloc = e->split ? ((size_t)e->m + 16 + 15) / 16 * 16 : 0;
-    e->packed_bytes = ends_alloc + w_alloc;
-    ce = cudaHostAlloc((void **)&e->h_packed, e->packed_bytes, cudaHostAllocMapped | cudaHostAllocPortable);
+    const size_t rec = 4ull * e->W;  // bytes per record in the ends stream
+    if (o.transfer_chunk_log2 > 40) return cleanup(fail(SGW_EINVAL, "transfer_chunk_log2 above 40"));
+    plan_stream(e->hs_ends, (size_t)e->m * rec, o.transfer_chunk_log2);
+    if (e->split) plan_stream(e->hs_w, (size_t)e->m, o.transfer_chunk_log2);
+    e->packed_bytes = e->hs_ends.bytes + e->hs_w.bytes;
+    HostStream *ends = &e->hs_ends;
+    ce = alloc_and_fill(e->hs_ends, e->hs_w, [&](HostStream &hs, size_t k) {
+      const size_t cb = size_t(1) << hs.shift;
+      if (&hs == ends) {  // edge words (packed, split-form destinations or records)
+        const uint64_t e0 = std::min<uint64_t>(e->m, (uint64_t)(k * cb / rec));
+        const uint64_t e1 = std::min<uint64_t>(e->m, (uint64_t)((k + 1) * cb / rec));
+        char *dst = hs.h[k];
+        if (pack) pack_range(g, e->pbits, (uint32_t *)dst, e0, e1);
+        else if (e->split) split_ends_range(g, (uint32_t *)dst, e0, e1);
+        else copy_records_range(g, dst, e0, e1);
+        const size_t used = (size_t)(e1 - e0) * rec;
+        memset(dst + used, 0, hs.size[k] - used);
+      } else {  // split form: weight bytes
+        const uint64_t e0 = std::min<uint64_t>(e->m, (uint64_t)(k * cb));
+        const uint64_t e1 = std::min<uint64_t>(e->m, (uint64_t)((k + 1) * cb));
+        split_weights_range(g, (uint8_t *)hs.h[k], e0, e1);
+        memset(hs.h[k] + (e1 - e0), 0, hs.size[k] - (size_t)(e1 - e0));
+      }
+    });
     if (ce != cudaSuccess) {
       cudaGetLastError();
-      e->h_packed = nullptr;
-      return cleanup(fail(SGW_ECUDA, "cudaHostAlloc(%zu) for the transfer copy: %s", e->packed_bytes,
+      return cleanup(fail(SGW_ECUDA, "cudaHostAlloc of the %zu-byte transfer copy: %s", e->packed_bytes,
                           cudaGetErrorString(ce)));
     }
-    char *hw = (char *)e->h_packed + ends_alloc;
-    if (pack) pack_into(g, e->pbits, e->h_packed);
-    else if (e->split) split_into(g, e->h_packed, (uint8_t *)hw);
-    else copy_records(g, e->h_packed);
-    memset((char *)e->h_packed + rec_bytes, 0, ends_alloc - rec_bytes);
-    if (e->split) memset(hw + e->m, 0, w_alloc - e->m);
-    e->h_src = e->h_packed;
-    e->h_wsrc = e->split ? hw : nullptr;
-    void *dp = nullptr;
-    ce = cudaHostGetDevicePointer(&dp, e->h_packed, 0);
-    if (ce != cudaSuccess) { cudaGetLastError(); return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce))); }
-    e->d_host_edges = (const uint32_t *)dp;
-    if (e->split) e->d_host_w16 = reinterpret_cast<const uint4 *>((const char *)dp + ends_alloc);
+    unsigned long long table[2 * kMaxHostChunks] = {};
+    HostStream *streams[2] = {&e->hs_ends, &e->hs_w};
+    for (int t = 0; t < 2; ++t)
+      for (size_t k = 0; k < streams[t]->h.size(); ++k) {
+        void *dp = nullptr;
+        ce = cudaHostGetDevicePointer(&dp, streams[t]->h[k], 0);
+        if (ce != cudaSuccess) {
+          cudaGetLastError();
+          return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce)));
+        }
+        streams[t]->d[k] = (unsigned long long)(uintptr_t)dp;
+        table[t * kMaxHostChunks + k] = streams[t]->d[k];
+      }
+    ce = cudaMemcpy(e->d_hct, table, sizeof(table), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) return cleanup(fail(SGW_ECUDA, "chunk table upload: %s", cudaGetErrorString(ce)));
   }
-  e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && e->d_host_edges &&
-                  ((uintptr_t)e->d_host_edges % 16 == 0);
+  e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && !e->hs_ends.h.empty();
   if (cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking) != cudaSuccess)
     return cleanup(fail(SGW_ECUDA, "stream creation"));
@@ -1374,7 +1505,7 @@ int sgw_engine_destroy(sgw_engine *e) {
   if (e->s_copy) cudaStreamDestroy(e->s_copy);
   if (e->h_ctl) cudaFreeHost(e->h_ctl);
   if (e->h_parts) cudaFreeHost(e->h_parts);
-  if (e->h_packed) cudaFreeHost(e->h_packed);
+  free_streams(e->hs_ends, e->hs_w);
   if (e->d_arena) cudaFree(e->d_arena);
   cudaGetLastError();
   delete e;

@@ -121,6 +121,31 @@ void split_into(const sgw_graph *g, uint32_t *ends, uint8_t *w8) {
   }
 }
 
+// The same transforms for edges [e0, e1), written from out[0] on (one chunk
+// of a transfer copy held in pieces).
+void pack_range(const sgw_graph *g, uint32_t nb, uint32_t *out, uint64_t e0, uint64_t e1) {
+  const uint32_t *ed = (const uint32_t *)g->edges;
+#pragma omp parallel for
+  for (int64_t i = (int64_t)e0; i < (int64_t)e1; ++i)
+    out[i - e0] = (ed[2 * size_t(i) + 1] << nb) | ed[2 * size_t(i)];
+}
+
+void split_ends_range(const sgw_graph *g, uint32_t *ends, uint64_t e0, uint64_t e1) {
+  const uint32_t *ed = (const uint32_t *)g->edges;
+#pragma omp parallel for
+  for (int64_t i = (int64_t)e0; i < (int64_t)e1; ++i) ends[i - e0] = ed[2 * size_t(i)];
+}
+
+void split_weights_range(const sgw_graph *g, uint8_t *w8, uint64_t e0, uint64_t e1) {
+  const uint32_t *ed = (const uint32_t *)g->edges;
+#pragma omp parallel for
+  for (int64_t i = (int64_t)e0; i < (int64_t)e1; ++i) w8[i - e0] = (uint8_t)ed[2 * size_t(i) + 1];
+}
+
+void copy_records_range(const sgw_graph *g, void *out, uint64_t e0, uint64_t e1) {
+  copy_bytes(out, (const char *)g->edges + e0 * g->esz, (e1 - e0) * g->esz);
+}
+
 bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint32_t *nbits) {
   *out = nullptr;
   uint32_t nb = 0;

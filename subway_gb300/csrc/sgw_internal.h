@@ -42,6 +42,11 @@ bool pack_weighted(const sgw_graph *g, uint32_t **out, size_t *alloc_bytes, uint
 bool pack_bits(const sgw_graph *g, uint32_t *nbits);
 // The same test given the largest weight (from max_weight).
 bool pack_bits_for(const sgw_graph *g, uint32_t wmax, uint32_t *nbits);
+// Edges [e0, e1) of the packed / split / record forms, written from out[0].
+void pack_range(const sgw_graph *g, uint32_t nbits, uint32_t *out, uint64_t e0, uint64_t e1);
+void split_ends_range(const sgw_graph *g, uint32_t *ends, uint64_t e0, uint64_t e1);
+void split_weights_range(const sgw_graph *g, uint8_t *w8, uint64_t e0, uint64_t e1);
+void copy_records_range(const sgw_graph *g, void *out, uint64_t e0, uint64_t e1);
 // Parallel memcpy in 64 MiB pieces.
 void copy_bytes(void *dst, const void *src, size_t bytes);
 void pack_into(const sgw_graph *g, uint32_t nbits, uint32_t *out);

@@ -804,6 +804,20 @@ __global__ void k_plan(const uint32_t *ptr, const uint32_t *queue, Ctl *ctl,
 }
 
 // ---- gather: host CSR -> device edge buffer -------------------------------
+// The engine's host transfer copy is a series of pinned chunks of 2^shift
+// bytes (allocated by two host threads at once, which halves the set-up of
+// a 21 GB copy); base is a device table of their device addresses.  A
+// 16-byte word or a record never straddles two chunks.
+struct HostChunks {
+  const unsigned long long *base;
+  uint32_t shift;
+};
+
+__device__ __forceinline__ const char *hc_at(const HostChunks &h, size_t byte) {
+  const char *c = reinterpret_cast<const char *>(__ldg(h.base + (byte >> h.shift)));
+  return c + (byte & ((size_t(1) << h.shift) - 1));
+}
+
 constexpr int kGatherThreads = 256;
 constexpr uint32_t kGatherTile = 2048;  // output edges per CTA tile
 
@@ -847,7 +861,7 @@ __device__ __forceinline__ uint32_t warp_last_le(const uint32_t *__restrict__ pt
 template <int W>
 __global__ void __launch_bounds__(kGatherThreads) k_gather(
     const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
-    const uint32_t *__restrict__ off, const uint32_t *__restrict__ host_edges,
+    const uint32_t *__restrict__ off, HostChunks host_edges,
     uint32_t *__restrict__ buf, uint32_t from, uint32_t size, uint32_t edge_from,
     uint32_t edge_count) {
   __shared__ uint32_t s_bpos[kGatherTile + 1];
@@ -883,8 +897,8 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(
         if (j < j1) {
           const uint32_t k = last_le(s_bpos, nsrc, j);
           const size_t h = (size_t)s_hpos[k] + (j - s_bpos[k]);
-          if (W == 1) e[u].x = host_edges[h];
-          else e[u] = reinterpret_cast<const uint2 *>(host_edges)[h];
+          if (W == 1) e[u].x = *reinterpret_cast<const uint32_t *>(hc_at(host_edges, h * 4));
+          else e[u] = *reinterpret_cast<const uint2 *>(hc_at(host_edges, h * 8));
         }
       }
 #pragma unroll
@@ -949,7 +963,7 @@ __device__ __forceinline__ uint32_t gather_scan(uint32_t nsrc, const uint32_t *s
 template <int RB>
 __device__ __forceinline__ void gather_copy(uint32_t total, uint32_t nsrc, uint32_t j0, const uint32_t *s_cs,
                                             const uint32_t *s_hlo, const uint32_t *s_len, const uint32_t *s_bpos,
-                                            const uint4 *__restrict__ host16, void *__restrict__ buf,
+                                            const HostChunks &host16, void *__restrict__ buf,
                                             uint8_t *s_bytes) {
   constexpr uint32_t R = 16 / RB;
   constexpr int U = 4;
@@ -965,7 +979,7 @@ __device__ __forceinline__ void gather_copy(uint32_t total, uint32_t nsrc, uint3
         const uint32_t c = s_hlo[k] / R + (j - s_cs[k]);
         kk[u] = k;
         cc[u] = c;
-        v[u] = host16[c];
+        v[u] = *reinterpret_cast<const uint4 *>(hc_at(host16, (size_t)c << 4));
       }
     }
 #pragma unroll
@@ -991,8 +1005,8 @@ __device__ __forceinline__ void gather_copy(uint32_t total, uint32_t nsrc, uint3
 template <int RB, bool WS>
 __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
     const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
-    const uint32_t *__restrict__ off, const uint4 *__restrict__ host16,
-    void *__restrict__ buf, const uint4 *__restrict__ host_w16, uint8_t *__restrict__ wbuf,
+    const uint32_t *__restrict__ off, HostChunks host16,
+    void *__restrict__ buf, HostChunks host_w16, uint8_t *__restrict__ wbuf,
     uint32_t from, uint32_t size, uint32_t edge_from, uint32_t edge_count) {
   __shared__ __align__(16) uint8_t s_bytes[WS ? kGatherTile : 16];
   __shared__ uint32_t s_bpos[kGatherTile + 1];

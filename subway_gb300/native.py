@@ -38,7 +38,7 @@ class EngineOpts(C.Structure):
                 ("chunk_edges", C.c_uint32), ("gather_ctas", C.c_uint32), ("num_buffers", C.c_uint32),
                 ("sched_inner", C.c_uint32), ("sched_active_permille", C.c_uint32),
                 ("sched_flags", C.c_uint32), ("sched_defer_permille", C.c_uint32),
-                ("reserved", C.c_uint32 * 2)]
+                ("transfer_chunk_log2", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class RunParams(C.Structure):

@@ -181,13 +181,62 @@ def test_hub_larger_than_budget(gpu, orc):
     w = (1 + (src * 7 + dst * 13) % 50).astype(np.uint32)
     edges = np.stack([dst.astype(np.uint32), w], 1)
     g = gpu.Graph.from_csr(npt, edges, True)
-    eng = gpu.Engine(g, budget_bytes=18 * n + 12 * 1024 + 1000 * 16)
+    eng = gpu.Engine(g, budget_bytes=18 * n + 13 * 1024 + 1000 * 16)
     assert eng.max_partition_size() < 2500
     for algo in ("bfs", "sssp", "sswp", "cc"):
         for mode in MODES:
             vals, _ = eng.run(algo, mode, 0)
             ref = _oracle(orc, g, algo, 0)
             assert np.array_equal(vals, ref), (algo, mode)
+
+
+@pytest.mark.parametrize("flags", ["", "NO_PACK", "SPLIT_WEIGHTS", "SCALAR_GATHER", "NO_PACK|SCALAR_GATHER"])
+def test_transfer_copy_in_small_chunks(gpu, orc, flags):
+    """The host transfer copy cut into dozens of 16 KiB pinned chunks (4 KiB
+    for the hub graph): rows and 16-byte words of the gather, whole-range
+    copies of the learned schedule and the pieces of a vertex larger than
+    the edge buffer all cross chunk boundaries, in every transfer form, and
+    give the oracle's answers."""
+    fl = 0
+    for f in filter(None, flags.split("|")):
+        fl |= getattr(gpu, "OPT_" + f)
+    g = gpu.Graph.rmat(14, 16, seed=12, weighted=True, wmax=64)
+    budget = 18 * g.n + 128 * 1024 + (g.m // 6) * 8 * 3
+    plain = gpu.Engine(g, budget_bytes=budget, flags=fl, transfer_chunk_log2=14)
+    learned = gpu.Engine(g, budget_bytes=budget, flags=fl, transfer_chunk_log2=14, num_buffers=3)
+    learned.set_policy("learned")
+    assert plain.max_partition_size() < g.m
+    src = int(g.pick_sources(1, seed=3)[0])
+    for algo in ("bfs", "sssp"):
+        ref = _oracle(orc, g, algo, src)
+        for mode in MODES:
+            for eng in (plain, learned):
+                vals, _ = eng.run(algo, mode, src)
+                assert np.array_equal(vals, ref), (algo, mode)
+    # a hub above the buffer, streamed in pieces that cross 4 KiB chunks
+    n = 3000
+    rng = np.random.default_rng(7)
+    hs = np.concatenate([np.zeros(2500, np.int64), rng.integers(0, n, 4000)])
+    hd = np.concatenate([np.arange(1, 2501), rng.integers(0, n, 4000)])
+    keep = (hs != hd) & (hs != n - 2)
+    pairs = np.unique(np.stack([hs[keep], hd[keep]], 1), axis=0)
+    npt = np.zeros(n + 1, np.uint32)
+    np.add.at(npt, pairs[:, 0] + 1, 1)
+    npt = np.cumsum(npt).astype(np.uint32)
+    w = (1 + (pairs[:, 0] * 7 + pairs[:, 1] * 13) % 50).astype(np.uint32)
+    hg = gpu.Graph.from_csr(npt, np.stack([pairs[:, 1].astype(np.uint32), w], 1), True)
+    heng = None
+    for extra in range(0, 64 * 1024, 1024):  # the smallest budget this transfer form fits
+        try:
+            heng = gpu.Engine(hg, budget_bytes=18 * n + 13 * 1024 + 1000 * 16 + extra, flags=fl,
+                              transfer_chunk_log2=12)
+            break
+        except gpu.SgwError:
+            continue
+    assert heng is not None and heng.max_partition_size() < 2500
+    for algo in ("bfs", "sssp"):
+        vals, _ = heng.run(algo, "async", 0)
+        assert np.array_equal(vals, _oracle(orc, hg, algo, 0)), algo
 
 
 # ---- PageRank ------------------------------------------------------------------
