@@ -151,12 +151,12 @@ typedef struct sgw_engine_opts {
                               (1 with SGW_OPT_NO_OVERLAP), at most 8          */
   /* Learned policy, async mode: a range whose predicted active-edge fraction
    * for the next global iteration is at least sched_active_permille / 1000
-   * (0 = 1) runs at most sched_inner inner iterations (0 = 2) now, since what
+   * (0 = 1) runs at most sched_inner inner iterations (0 = 3) now, since what
    * further passes would settle is likely to be redone when it is relaxed
    * again; other ranges run to local convergence.  Without
    * SGW_SCHED_CAP_COMPACT the cap only covers ranges that stay in their edge
    * buffer (their leftover sources cost no transfer).
-   * sched_active_permille > 1000 turns the cap off.  Defaults: 2, 1,
+   * sched_active_permille > 1000 turns the cap off.  Defaults: 3, 1,
    * SGW_SCHED_CAP_COMPACT. */
   uint32_t sched_inner;
   uint32_t sched_active_permille;

@@ -244,6 +244,11 @@ void plan_stream(HostStream &hs, size_t bytes, uint32_t log2_chunk) {
 // same bytes (21 GiB on a GB300 host: 0.78 s against 1.27 s; more threads
 // did not help), while filling a chunk takes all host cores for a fraction
 // of its allocation time.
+#ifndef SGW_ALLOC_THREADS
+#define SGW_ALLOC_THREADS 2
+#endif
+constexpr int kAllocThreads = SGW_ALLOC_THREADS;
+
 template <class Fill>
 cudaError_t alloc_and_fill(HostStream &a, HostStream &b, Fill fill) {
   std::vector<std::pair<HostStream *, size_t>> items;
@@ -252,9 +257,10 @@ cudaError_t alloc_and_fill(HostStream &a, HostStream &b, Fill fill) {
   std::unique_ptr<std::atomic<int>[]> state(new std::atomic<int>[items.size()]);  // 0 pending, 1 ready, 2 failed
   for (size_t i = 0; i < items.size(); ++i) state[i].store(0);
   std::atomic<int> stop{0};
-  cudaError_t err[2] = {cudaSuccess, cudaSuccess};
+  cudaError_t err[kAllocThreads];
+  for (int t = 0; t < kAllocThreads; ++t) err[t] = cudaSuccess;
   auto work = [&](int t) {
-    for (size_t i = (size_t)t; i < items.size(); i += 2) {
+    for (size_t i = (size_t)t; i < items.size(); i += kAllocThreads) {
       if (stop.load()) { state[i].store(2); continue; }
       HostStream &hs = *items[i].first;
       const size_t k = items[i].second;
@@ -270,16 +276,18 @@ cudaError_t alloc_and_fill(HostStream &a, HostStream &b, Fill fill) {
       state[i].store(1);
     }
   };
-  std::thread t0(work, 0), t1(work, 1);
+  std::vector<std::thread> th;
+  for (int t = 0; t < kAllocThreads; ++t) th.emplace_back(work, t);
   for (size_t i = 0; i < items.size(); ++i) {
     int st;
     while ((st = state[i].load()) == 0) std::this_thread::yield();
     if (st != 1) break;
     fill(*items[i].first, items[i].second);
   }
-  t0.join();
-  t1.join();
-  return err[0] != cudaSuccess ? err[0] : err[1];
+  for (auto &t : th) t.join();
+  for (int t = 0; t < kAllocThreads; ++t)
+    if (err[t] != cudaSuccess) return err[t];
+  return cudaSuccess;
 }
 
 // Frees both streams' chunks, two at a time (as they were allocated).
@@ -1185,7 +1193,7 @@ int process_iteration_ranges(sgw_engine *e) {
       float pred = 0.0f;
       for (uint32_t s = j.s; s < j.s_end; ++s) pred = std::max(pred, e->h_rstat[s].pred);
       const bool cappable = kept || (e->opts.sched_flags & SGW_SCHED_CAP_COMPACT);
-      e->range_inner_cap = cappable && (double)pred >= thr ? (e->opts.sched_inner ? e->opts.sched_inner : 2u) : 0u;
+      e->range_inner_cap = cappable && (double)pred >= thr ? (e->opts.sched_inner ? e->opts.sched_inner : 3u) : 0u;
       const int st = process_resident(e, q, (uint32_t)j.buf, &inner);
       e->cur_streamed = 0;
       e->range_inner_cap = 0;
@@ -1232,7 +1240,7 @@ void sgw_engine_opts_default(sgw_engine_opts *o) {
   o->inner_batch = 8;
   o->tile_degree_max = 256;
   o->chunk_edges = 1024;
-  o->sched_inner = 2;
+  o->sched_inner = 3;
   o->sched_active_permille = 1;
   o->sched_flags = SGW_SCHED_CAP_COMPACT;
 }

@@ -105,10 +105,16 @@ void copy_records(const sgw_graph *g, void *out) { copy_bytes(out, g->edges, siz
 
 uint32_t max_weight(const sgw_graph *g) {
   if (!g->weighted || g->m == 0) return 0;
+  const bool cacheable = g->owns || g->map_base;
+  if (cacheable) {
+    const int64_t c = g->wmax_cache.load(std::memory_order_relaxed);
+    if (c >= 0) return (uint32_t)c;
+  }
   const uint32_t *ed = (const uint32_t *)g->edges;
   uint32_t wmax = 0;
 #pragma omp parallel for reduction(max : wmax)
   for (int64_t i = 0; i < (int64_t)g->m; ++i) wmax = std::max(wmax, ed[2 * size_t(i) + 1]);
+  if (cacheable) g->wmax_cache.store(wmax, std::memory_order_relaxed);
   return wmax;
 }
 

@@ -2,6 +2,7 @@
 // libsubwaygb.  Not part of the public ABI.
 #pragma once
 
+#include <atomic>
 #include <stddef.h>
 #include <stdint.h>
 
@@ -18,6 +19,11 @@ struct sgw_graph {
   size_t edges_bytes_alloc = 0;   // rounded allocation size of edges
   void *map_base = nullptr;       // sgw_graph_map: the file mapping holding edges
   size_t map_len = 0;
+  // Largest edge weight, found by the first engine created on a graph whose
+  // records the library owns or maps read-only (-1: not known yet).  A
+  // caller's arrays (sgw_graph_from_csr) may change between engines, so for
+  // those it is found again every time.
+  mutable std::atomic<int64_t> wmax_cache{-1};
 };
 
 namespace sgw {
