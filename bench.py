@@ -238,6 +238,10 @@ def probe_link(N, dev):
 # before each launch, so these are cold-cache figures).  A full-size launch's
 # traffic is the ratio times its algorithmic bytes: an estimate, not a count.
 DRAM_PER_ALGO_BYTE = {"gather": 0.73, "relax": 1.06, "generate": 2.23}
+# Host-link bytes (L2 sectors filled from host memory) per algorithmic byte of
+# the gather, from a one-kernel capture over every gather of one measured
+# RMAT-24 / 1 GB run (profiles/k_gather_v_rmat24_sssp_async_1gb.md).
+LINK_PER_ALGO_BYTE = {"gather": 1.063}
 
 
 def run_ours(a, dist):
@@ -414,6 +418,7 @@ def run_ours(a, dist):
         roof[name] = {"bound": bound, "achieved": round(ach, 2), "peak": round(peak, 1), "unit": "GB/s",
                       "frac": round(ach / peak, 4) if peak else None,
                       "traffic": int(DRAM_PER_ALGO_BYTE[name] * bpl), "launches": launches,
+                      "link_traffic": int(LINK_PER_ALGO_BYTE[name] * bpl) if name in LINK_PER_ALGO_BYTE else None,
                       "ms_per_launch": round(ms / max(launches, 1), 4), "bytes_per_launch": round(bpl),
                       "peak_source": src}
     stream_ms = sum(s["ms_stream"] for s in steps)
