@@ -678,15 +678,15 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
   const HostChunks h16{e->d_hct, e->hs_ends.shift};
   const HostChunks hw16{e->d_hct + kMaxHostChunks, e->hs_w.shift};
   if (e->vec_gather && e->W == 1 && e->use_w)  // split form: destination words and weight bytes
-    k_gather_v<4, true><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+    k_gather_v<4, true><<<grid, kGatherThreads, kGatherSmemBytes, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
                                                         hw16, e->d_wbuf[b], q.from, q.size,
                                                         q.edge_from, (uint32_t)q.edge_count);
   else if (e->vec_gather && e->W == 1)
-    k_gather_v<4, false><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+    k_gather_v<4, false><<<grid, kGatherThreads, kGatherSmemBytes, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
                                                          hw16, nullptr, q.from, q.size, q.edge_from,
                                                          (uint32_t)q.edge_count);
   else if (e->vec_gather)
-    k_gather_v<8, false><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
+    k_gather_v<8, false><<<grid, kGatherThreads, kGatherSmemBytes, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
                                                          hw16, nullptr, q.from, q.size, q.edge_from,
                                                          (uint32_t)q.edge_count);
   else if (e->W == 1)
@@ -1470,6 +1470,16 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
     if (ce != cudaSuccess) return cleanup(fail(SGW_ECUDA, "chunk table upload: %s", cudaGetErrorString(ce)));
   }
   e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && !e->hs_ends.h.empty();
+  if (kGatherSmemBytes > 48 * 1024 &&
+      (cudaFuncSetAttribute(k_gather_v<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)kGatherSmemBytes) != cudaSuccess ||
+       cudaFuncSetAttribute(k_gather_v<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)kGatherSmemBytes) != cudaSuccess ||
+       cudaFuncSetAttribute(k_gather_v<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)kGatherSmemBytes) != cudaSuccess)) {
+    cudaGetLastError();
+    return cleanup(fail(SGW_ECUDA, "gather shared memory of %zu bytes refused", kGatherSmemBytes));
+  }
   if (cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking) != cudaSuccess)
     return cleanup(fail(SGW_ECUDA, "stream creation"));

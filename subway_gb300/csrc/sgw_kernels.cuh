@@ -819,7 +819,14 @@ __device__ __forceinline__ const char *hc_at(const HostChunks &h, size_t byte) {
 }
 
 constexpr int kGatherThreads = 256;
-constexpr uint32_t kGatherTile = 2048;  // output edges per CTA tile
+// Output edges per CTA tile of the vectorised gather (its shared memory is
+// dynamic: 16 bytes per tile edge plus the weight bytes); the scalar gather
+// keeps 2048.
+#ifndef SGW_GATHER_TILE
+#define SGW_GATHER_TILE 2048
+#endif
+constexpr uint32_t kGatherTile = SGW_GATHER_TILE;
+constexpr uint32_t kScalarGatherTile = 2048;
 
 // Index of the last element <= x in a[0..len) (a non-decreasing, a[0] <= x).
 __device__ __forceinline__ uint32_t last_le(const uint32_t *a, uint32_t len, uint32_t x) {
@@ -864,13 +871,13 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(
     const uint32_t *__restrict__ off, HostChunks host_edges,
     uint32_t *__restrict__ buf, uint32_t from, uint32_t size, uint32_t edge_from,
     uint32_t edge_count) {
-  __shared__ uint32_t s_bpos[kGatherTile + 1];
-  __shared__ uint32_t s_hpos[kGatherTile + 1];
+  __shared__ uint32_t s_bpos[kScalarGatherTile + 1];
+  __shared__ uint32_t s_hpos[kScalarGatherTile + 1];
   __shared__ uint32_t s_first, s_last;
-  const uint32_t ntiles = (edge_count + kGatherTile - 1) / kGatherTile;
+  const uint32_t ntiles = (edge_count + kScalarGatherTile - 1) / kScalarGatherTile;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const uint32_t j0 = t * kGatherTile;
-    const uint32_t j1 = min(edge_count, j0 + kGatherTile);
+    const uint32_t j0 = t * kScalarGatherTile;
+    const uint32_t j1 = min(edge_count, j0 + kScalarGatherTile);
     // sources covering [j0, j1): warp 0 finds the first, warp 1 the last
     if (threadIdx.x < 64) {
       const int lane = threadIdx.x & 31;
@@ -1002,18 +1009,24 @@ __device__ __forceinline__ void gather_copy(uint32_t total, uint32_t nsrc, uint3
   }
 }
 
+// Dynamic shared memory of k_gather_v: four u32 arrays of kGatherTile + 1
+// entries, the scan partials, then (16-byte aligned) the tile's weight bytes.
+constexpr size_t kGatherBytesOff = ((4 * (kGatherTile + 1) + kGatherThreads + 1) * 4 + 15) / 16 * 16;
+constexpr size_t kGatherSmemBytes = kGatherBytesOff + kGatherTile;
+
 template <int RB, bool WS>
 __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
     const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
     const uint32_t *__restrict__ off, HostChunks host16,
     void *__restrict__ buf, HostChunks host_w16, uint8_t *__restrict__ wbuf,
     uint32_t from, uint32_t size, uint32_t edge_from, uint32_t edge_count) {
-  __shared__ __align__(16) uint8_t s_bytes[WS ? kGatherTile : 16];
-  __shared__ uint32_t s_bpos[kGatherTile + 1];
-  __shared__ uint32_t s_hlo[kGatherTile + 1];
-  __shared__ uint32_t s_len[kGatherTile + 1];
-  __shared__ uint32_t s_cs[kGatherTile + 1];
-  __shared__ uint32_t s_part[kGatherThreads + 1];
+  extern __shared__ __align__(16) unsigned char g_gather_smem[];
+  uint32_t *const s_bpos = reinterpret_cast<uint32_t *>(g_gather_smem);
+  uint32_t *const s_hlo = s_bpos + (kGatherTile + 1);
+  uint32_t *const s_len = s_hlo + (kGatherTile + 1);
+  uint32_t *const s_cs = s_len + (kGatherTile + 1);
+  uint32_t *const s_part = s_cs + (kGatherTile + 1);
+  uint8_t *const s_bytes = g_gather_smem + kGatherBytesOff;
   __shared__ uint32_t s_first, s_last;
   const uint32_t ntiles = (edge_count + kGatherTile - 1) / kGatherTile;
   const int tid = threadIdx.x;
