@@ -527,12 +527,8 @@ int launch_select(sgw_engine *e) {
   const int algo = e->params.algo;
   size_t slot = 0;
   TRY(prof_begin(e, K_GENERATE, e->s_comp, &slot));
-  CK(cudaMemsetAsync(&e->d_ctl->sel_lo, 0xff, sizeof(uint32_t), e->s_comp));
-  CK(cudaMemsetAsync(&e->d_ctl->sel_hi, 0, sizeof(uint32_t), e->s_comp));
   CK(cudaMemsetAsync(e->d_sel_hist, 0, sizeof(unsigned long long) * kSelBins, e->s_comp));
   const uint32_t grid = grid_for(e, (e->n + 15) / 16, 256);
-  k_select_range<<<grid, 256, 0, e->s_comp>>>(e->n, algo, e->d_l1, e->d_l2, e->d_off, e->d_value, e->d_ctl);
-  CK(cudaGetLastError());
   k_select_hist<<<grid, 256, 0, e->s_comp>>>(e->n, algo, e->d_l1, e->d_l2, e->d_off, e->d_value, e->d_ctl,
                                              e->d_sel_hist);
   CK(cudaGetLastError());
@@ -540,7 +536,7 @@ int launch_select(sgw_engine *e) {
   k_select_pick<<<1, kSelBins / 4, 0, e->s_comp>>>(algo, e->d_sel_hist, target, e->d_ctl);
   CK(cudaGetLastError());
   TRY(prof_end(e, e->s_comp, slot));
-  e->stats.launches += 3;
+  e->stats.launches += 2;
   return SGW_OK;
 }
 

@@ -46,8 +46,7 @@ struct Ctl {
   uint32_t iters_run;        // inner iterations that did work
   uint32_t hub_active;       // single-vertex partition: the source was dirty
   uint32_t hub_value;        // single-vertex partition: its value
-  uint32_t sel_lo, sel_hi;   // deferral: value range of the pushable active vertices
-  uint32_t sel_bin;          //   and the last value bin selected this iteration
+  uint32_t sel_bin;          // deferral: the last value bin selected this iteration
   uint32_t iters_total;      // inner iterations that did work, whole run
   unsigned long long reached_edges;
   unsigned long long relaxed_edges;
@@ -244,17 +243,18 @@ __device__ __forceinline__ bool pushable(int algo, uint32_t v) {
   return true;
 }
 
-// Deferral bins: kSelBins equal slices of [lo, hi]; min-algorithms take the
-// lowest values first, SSWP (max) the highest.  Values outside [lo, hi] (set
-// after the histogram was taken) count as selected when they are better.
+// Deferral bins: fixed and monotone in the value, so one pass builds the
+// histogram: values below 64 get a bin each, larger ones 32 bins per power of
+// two (bin < 896 of kSelBins).  Min-algorithms take the lowest bins first,
+// SSWP (max) the highest.
 constexpr uint32_t kSelBins = 1024;
-__device__ __forceinline__ uint32_t sel_bin_of(uint32_t v, uint32_t lo, uint32_t hi) {
-  return (uint32_t)(((unsigned long long)(v - lo) * kSelBins) / ((unsigned long long)(hi - lo) + 1ull));
+__device__ __forceinline__ uint32_t sel_bin_of(uint32_t v) {
+  if (v < 64u) return v;
+  const uint32_t e = 31u - (uint32_t)__clz((int)v);
+  return 64u + (e - 6u) * 32u + ((v >> (e - 5u)) & 31u);
 }
-__device__ __forceinline__ bool selected(int algo, uint32_t v, uint32_t lo, uint32_t hi, uint32_t bin) {
-  if (v < lo) return algo != SGW_SSWP;
-  if (v > hi) return algo == SGW_SSWP;
-  const uint32_t b = sel_bin_of(v, lo, hi);
+__device__ __forceinline__ bool selected(int algo, uint32_t v, uint32_t bin) {
+  const uint32_t b = sel_bin_of(v);
   return algo == SGW_SSWP ? b >= bin : b <= bin;
 }
 
@@ -288,12 +288,8 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
   uint32_t keepmask[kGenRounds];
   double push[PR ? kGenRounds : 1];
   uint32_t wcount = 0, wedges = 0, seen = 0;
-  uint32_t sel_lo = 0, sel_hi = 0, sel_bin = 0;
-  if (!PR && (a.sel_mode & 2)) {
-    sel_lo = a.ctl->sel_lo;
-    sel_hi = a.ctl->sel_hi;
-    sel_bin = a.ctl->sel_bin;
-  }
+  uint32_t sel_bin = 0;
+  if (!PR && (a.sel_mode & 2)) sel_bin = a.ctl->sel_bin;
 #pragma unroll
   for (int r = 0; r < kGenRounds; ++r) {
     const uint32_t v = wbase + r * 32 + lane;
@@ -319,7 +315,7 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
         if (a.sel_mode && !drop) {
           const uint32_t val = a.value[v];
           if (!pushable(a.algo, val)) drop = (a.sel_mode & 1) != 0;
-          else if ((a.sel_mode & 2) && !selected(a.algo, val, sel_lo, sel_hi, sel_bin)) defer = true;
+          else if ((a.sel_mode & 2) && !selected(a.algo, val, sel_bin)) defer = true;
         }
         if (!defer && (a.consume || drop)) { a.l1[v] = 0; a.l2[v] = 0; }
         if (drop) d = 0;
@@ -413,12 +409,8 @@ struct GenLane {
 
 // Selection for the lane's 16 vertices starting at v0.
 __device__ __forceinline__ void gen_lane(const GenArgs &a, uint32_t v0, bool full, GenLane &L) {
-  uint32_t sel_lo = 0, sel_hi = 0, sel_bin = 0;
-  if (a.sel_mode & 2) {
-    sel_lo = a.ctl->sel_lo;
-    sel_hi = a.ctl->sel_hi;
-    sel_bin = a.ctl->sel_bin;
-  }
+  uint32_t sel_bin = 0;
+  if (a.sel_mode & 2) sel_bin = a.ctl->sel_bin;
   if (full) {
     const uint4 x = *reinterpret_cast<const uint4 *>(a.l1 + v0);
     const uint4 y = *reinterpret_cast<const uint4 *>(a.l2 + v0);
@@ -469,7 +461,7 @@ __device__ __forceinline__ void gen_lane(const GenArgs &a, uint32_t v0, bool ful
     bool drop = d == 0, defer = false;
     if (a.sel_mode && !drop) {
       if (!pushable(a.algo, val[k])) drop = (a.sel_mode & 1) != 0;
-      else if ((a.sel_mode & 2) && !selected(a.algo, val[k], sel_lo, sel_hi, sel_bin)) defer = true;
+      else if ((a.sel_mode & 2) && !selected(a.algo, val[k], sel_bin)) defer = true;
     }
     if (!defer && (a.consume || drop)) L.clearmask |= 1u << k;
     if (!drop && !defer) {
@@ -638,10 +630,10 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_write(GenArgs a) {
 }
 
 // ---- frontier deferral (learned policy) --------------------------------------
-// Before a generate, three small passes pick how much of the frontier to take:
-// the value range of the pushable active vertices, a histogram of their
-// out-degrees over kSelBins value bins, and the bin at which the cumulative
-// degree reaches the target (lowest values first; highest for SSWP).  The
+// Before a generate, two small passes pick how much of the frontier to take:
+// a histogram of the pushable active vertices' out-degrees over the fixed
+// value bins, and the bin at which the cumulative degree reaches the target
+// (lowest values first; highest for SSWP).  The
 // generate then queues only the selected vertices; the rest keep their labels
 // for a later iteration.  Relaxing far vertices first wastes their edges'
 // transfer when they improve again later; this is the delta-stepping idea
@@ -677,21 +669,6 @@ __device__ __forceinline__ void for_sel_candidates(uint32_t n, int algo, const u
     if ((l1[v] | l2[v]) != 0) visit(v);
 }
 
-__global__ void __launch_bounds__(256) k_select_range(uint32_t n, int algo, const uint8_t *l1, const uint8_t *l2,
-                                                      const uint32_t *off, const uint32_t *value, Ctl *ctl) {
-  uint32_t lo = 0xffffffffu, hi = 0u;
-  for_sel_candidates(n, algo, l1, l2, off, value, [&](uint32_t val, uint32_t) {
-    lo = min(lo, val);
-    hi = max(hi, val);
-  });
-  lo = __reduce_min_sync(0xffffffffu, lo);
-  hi = __reduce_max_sync(0xffffffffu, hi);
-  if ((threadIdx.x & 31) == 0 && lo <= hi) {
-    atomicMin(&ctl->sel_lo, lo);
-    atomicMax(&ctl->sel_hi, hi);
-  }
-}
-
 // Per-CTA bins in shared memory (per-CTA sums stay below m < 2^32), added
 // into 64-bit global bins at the end.
 __global__ void __launch_bounds__(256) k_select_hist(uint32_t n, int algo, const uint8_t *l1, const uint8_t *l2,
@@ -700,10 +677,8 @@ __global__ void __launch_bounds__(256) k_select_hist(uint32_t n, int algo, const
   __shared__ uint32_t s_hist[kSelBins];
   for (uint32_t i = threadIdx.x; i < kSelBins; i += blockDim.x) s_hist[i] = 0u;
   __syncthreads();
-  const uint32_t lo = ctl->sel_lo, hi = ctl->sel_hi;
-  if (lo <= hi)
-    for_sel_candidates(n, algo, l1, l2, off, value,
-                       [&](uint32_t val, uint32_t deg) { atomicAdd(&s_hist[sel_bin_of(val, lo, hi)], deg); });
+  for_sel_candidates(n, algo, l1, l2, off, value,
+                     [&](uint32_t val, uint32_t deg) { atomicAdd(&s_hist[sel_bin_of(val)], deg); });
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < kSelBins; i += blockDim.x)
     if (s_hist[i]) atomicAdd(&hist[i], (unsigned long long)s_hist[i]);
