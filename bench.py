@@ -286,10 +286,11 @@ def run_ours(a, dist):
         from oracle import oracle
         e = g.edges if weighted else g.ends
         deg = g.out_degree()
+        npt = np.ascontiguousarray(g.node_pointer, dtype=np.uint64)  # the oracle's width, once
         secs, reached_cpu = 0.0, 0
         for s in dict.fromkeys(sources):
             t = time.perf_counter()
-            ref = oracle.run(a.algo, g.node_pointer, e, s, parallel=True)
+            ref = oracle.run(a.algo, npt, e, s, parallel=True)
             secs += time.perf_counter() - t
             want = int(deg[ref != (0 if a.algo == "sswp" else INF)].astype(np.uint64).sum())
             reached_cpu += want

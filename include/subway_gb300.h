@@ -60,16 +60,23 @@ const char *sgw_last_error(void);
  * OutEdge {u32 end} (4 B) and OutEdgeWeighted {u32 end; u32 w8} (8 B)
  * (shared/globals.hpp:33-40).  Binary CSR files are
  * [u32 n][u32 m][u32 nodePointer x n][edge x m]
- * (shared/graph.cu:39-52, tools/converter.cpp:88-95).                       */
+ * (shared/graph.cu:39-52, tools/converter.cpp:88-95).  Graphs of 2^32 edges
+ * or more, which that u32 header cannot describe, use .bcsr64 / .bwcsr64:
+ * [u64 n][u64 m][u64 nodePointer x n][edge x m], the same records, every
+ * field 8-byte aligned (no counterpart in the reference).  In memory a graph
+ * keeps u32 node pointers below 2^32 edges and u64 ones from there on;
+ * sgw_graph_node_pointer / sgw_graph_node_pointer64 return whichever it has
+ * (the other is NULL).  Vertex ids stay u32 and out-degrees below 2^32.      */
 
 /* Replaces Graph<E>::ReadGraph / GraphPR<E>::ReadGraph
  * (shared/graph.cu:32-197, :229-394).  The type is chosen by the extension:
- * .bcsr/.el unweighted, .bwcsr/.wel weighted (shared/graph.cu:37-53).
+ * .bcsr/.bcsr64/.el unweighted, .bwcsr/.bwcsr64/.wel weighted
+ * (shared/graph.cu:37-53).
  * out-degree is derived for every vertex (the reference leaves
  * outDegree[n-2] unset, shared/graph.cu:179-181). */
 int sgw_graph_load(const char *path, sgw_graph **out);
 
-/* Maps a .bcsr/.bwcsr file instead of reading it (shared/graph.cu:41-51
+/* Maps a .bcsr/.bwcsr(64) file instead of reading it (shared/graph.cu:41-51
  * freads the whole file into pinned memory): the edge records stay in the
  * read-only file mapping, shared with the page cache, and only the n node
  * pointers are copied (plus the sentinel node_pointer[n] = m, which the file
@@ -91,15 +98,23 @@ int sgw_graph_map(const char *path, sgw_graph **out);
  * Graph<E>::ReadGraph fills (shared/graph.cu:46-51). */
 int sgw_graph_from_csr(uint32_t n, uint32_t m, const uint32_t *node_pointer,
                        const void *edges, int weighted, sgw_graph **out);
+/* The same with u64 node pointers (any m; the arrays are borrowed as
+ * above).  Engines on such a graph take the wide path whatever m is. */
+int sgw_graph_from_csr64(uint32_t n, uint64_t m, const uint64_t *node_pointer,
+                         const void *edges, int weighted, sgw_graph **out);
 
+/* SGW_ERANGE for a graph of 2^32 edges or more: use sgw_graph_info64. */
 int sgw_graph_info(const sgw_graph *g, uint32_t *n, uint32_t *m, int *weighted);
+int sgw_graph_info64(const sgw_graph *g, uint32_t *n, uint64_t *m, int *weighted);
 const uint32_t *sgw_graph_node_pointer(const sgw_graph *g);
+const uint64_t *sgw_graph_node_pointer64(const sgw_graph *g);
 const void *sgw_graph_edges(const sgw_graph *g);
 /* outDegree[i] = nodePointer[i+1] - nodePointer[i] for all i
  * (shared/graph.cu:177-181 with every entry written). */
 int sgw_graph_out_degree(const sgw_graph *g, uint32_t *out_degree);
-/* Writes .bcsr/.bwcsr (tools/converter.cpp:88-95, :157-164) or .el/.wel
- * text, chosen by extension. */
+/* Writes .bcsr/.bwcsr (tools/converter.cpp:88-95, :157-164), .bcsr64 /
+ * .bwcsr64, or .el/.wel text, chosen by extension; SGW_ERANGE for a u32
+ * file of a graph with 2^32 edges or more. */
 int sgw_graph_save(const sgw_graph *g, const char *path);
 void sgw_graph_free(sgw_graph *g);
 
@@ -173,7 +188,12 @@ typedef struct sgw_engine_opts {
    * 2^transfer_chunk_log2 bytes (0 = 30, i.e. 1 GiB; at most 64 chunks per
    * stream, larger chunks if needed), two chunks at a time. */
   uint32_t transfer_chunk_log2;
-  uint32_t reserved;
+  /* Most edges one generate queues (BFS/SSSP/SSWP/CC): the active vertices
+   * of whole 4096-vertex tiles, in vertex order, up to this many edges (the
+   * first tile with edges always); the rest stay active for the next
+   * iteration, which the answers do not depend on.  0 = 2^31 for graphs of
+   * 2^32 edges or more (queue positions are u32), else no limit. */
+  uint32_t generate_edge_limit;
 } sgw_engine_opts;
 
 void sgw_engine_opts_default(sgw_engine_opts *opts);

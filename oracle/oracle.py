@@ -2,8 +2,10 @@
 
 TEST INFRASTRUCTURE: imported only by the tests, the smoke check and the
 benchmark's CPU-baseline leg.  Functions take a host CSR as numpy arrays
-(node_pointer of n+1 u32, edges of m u32 or (m, 2) u32) and return numpy
-arrays of final values.
+(node_pointer of n+1 u32 or u64, edges of m u32 or (m, 2) u32) and return
+numpy arrays of final values.  The C side takes u64 node pointers: u32
+arrays are widened on every call, so callers that repeat calls on a large
+graph widen once (np.uint64) and pass that.
 """
 from __future__ import annotations
 
@@ -49,7 +51,7 @@ def lib():
 
 
 def _csr(node_pointer, edges):
-    npa = np.ascontiguousarray(node_pointer, dtype=np.uint32)
+    npa = np.ascontiguousarray(node_pointer, dtype=np.uint64)
     eda = np.ascontiguousarray(edges, dtype=np.uint32)
     stride = 2 if eda.ndim == 2 else 1
     return npa, eda, stride
@@ -124,15 +126,22 @@ def rmat_write(path, scale, edge_factor=16, seed=1, weighted=False, wmax=64, a=0
 
 
 def read_csr(path):
-    """(node_pointer[n+1], edges) of a .bcsr/.bwcsr file; edges map the file in place."""
-    hdr = np.fromfile(path, dtype=np.uint32, count=2)
-    n, m = int(hdr[0]), int(hdr[1])
-    npa = np.empty(n + 1, np.uint32)
-    npa[:n] = np.memmap(path, dtype=np.uint32, mode="r", offset=8, shape=(n,))
+    """(node_pointer[n+1], edges) of a .bcsr/.bwcsr file (u32 node pointers) or of a
+    .bcsr64/.bwcsr64 file (u64); edges map the file in place."""
+    path = str(path)
+    wide = path.endswith("64")
+    if wide:
+        n, m = (int(x) for x in np.fromfile(path, dtype=np.uint64, count=2))
+        hdr, npw, npt = 16, 8, np.uint64
+    else:
+        n, m = (int(x) for x in np.fromfile(path, dtype=np.uint32, count=2))
+        hdr, npw, npt = 8, 4, np.uint32
+    npa = np.empty(n + 1, npt)
+    npa[:n] = np.memmap(path, dtype=npt, mode="r", offset=hdr, shape=(n,))
     npa[n] = m
-    weighted = str(path).endswith(".bwcsr")
+    weighted = path.endswith((".bwcsr", ".bwcsr64"))
     shape = (m, 2) if weighted else (m,)
-    edges = np.memmap(path, dtype=np.uint32, mode="r", offset=8 + 4 * n, shape=shape) if m else \
+    edges = np.memmap(path, dtype=np.uint32, mode="r", offset=hdr + npw * n, shape=shape) if m else \
         np.zeros(shape, np.uint32)
     return npa, edges
 

@@ -28,6 +28,9 @@
  *
  * Edge records are `stride` u32 words: word 0 the destination, word 1 the
  * weight when stride == 2 (OutEdge / OutEdgeWeighted, shared/globals.hpp:33-40).
+ * Node pointers are u64 (n + 1 entries; the reference's are u32,
+ * shared/graph.cu:46), so graphs of 2^32 edges or more are checked too; the
+ * Python wrapper widens u32 arrays.
  */
 #include <math.h>
 #include <omp.h>
@@ -43,7 +46,7 @@
 /* ------------------------------------------------------------------------ */
 
 /* Queue BFS. */
-int orc_bfs(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
+int orc_bfs(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride,
             uint32_t src, uint32_t *out) {
   uint32_t *q = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
   if (!q) return -1;
@@ -53,7 +56,7 @@ int orc_bfs(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
   q[tail++] = src;
   while (head < tail) {
     uint32_t u = q[head++];
-    for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+    for (uint64_t i = np[u]; i < np[u + 1]; ++i) {
       uint32_t v = ed[(size_t)i * stride];
       if (out[v] == ORC_INF) {
         out[v] = out[u] + 1;
@@ -109,7 +112,7 @@ static uint64_t heap_pop(heap_t *h) {
 
 /* Dijkstra (min-plus).  Distances wrap in u32 exactly like the reference's
  * `sourceWeight + w8` (they never come near 2^32 for the supported weights). */
-int orc_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
+int orc_sssp(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride,
              uint32_t src, uint32_t *out) {
   if (stride != 2) return -2;
   heap_t h = {0, 0, 0};
@@ -120,7 +123,7 @@ int orc_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride
     uint64_t x = heap_pop(&h);
     uint32_t d = (uint32_t)(x >> 32), u = (uint32_t)x;
     if (d != out[u]) continue;
-    for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+    for (uint64_t i = np[u]; i < np[u + 1]; ++i) {
       uint32_t v = ed[(size_t)i * 2], w = ed[(size_t)i * 2 + 1];
       uint32_t c = d + w;
       if (c < out[v]) {
@@ -134,7 +137,7 @@ int orc_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride
 }
 
 /* Widest path (max-min) by a max-heap Dijkstra; unreached stay 0. */
-int orc_sswp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
+int orc_sswp(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride,
              uint32_t src, uint32_t *out) {
   if (stride != 2) return -2;
   heap_t h = {0, 0, 0};
@@ -146,7 +149,7 @@ int orc_sswp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride
     uint64_t x = heap_pop(&h);
     uint32_t wdt = ~(uint32_t)(x >> 32), u = (uint32_t)x;
     if (wdt != out[u]) continue;
-    for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+    for (uint64_t i = np[u]; i < np[u + 1]; ++i) {
       uint32_t v = ed[(size_t)i * 2], w = ed[(size_t)i * 2 + 1];
       uint32_t c = wdt < w ? wdt : w;
       if (c > out[v]) {
@@ -161,7 +164,7 @@ int orc_sswp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride
 
 /* value[v] = min id among the vertices that reach v along out-edges:
  * ascending sources, each BFS only over still-unlabelled vertices. */
-int orc_cc(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
+int orc_cc(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride,
            uint32_t *out) {
   uint32_t *q = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
   if (!q) return -1;
@@ -174,7 +177,7 @@ int orc_cc(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
     q[tail++] = s;
     while (head < tail) {
       uint32_t u = q[head++];
-      for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+      for (uint64_t i = np[u]; i < np[u + 1]; ++i) {
         uint32_t v = ed[(size_t)i * stride];
         if (out[v] == unset) {
           out[v] = s;
@@ -191,7 +194,7 @@ int orc_cc(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
  * vertex with delta > acc moves its delta into its value and pushes
  * damping * delta / outdeg to each out-neighbour; pushes land in the next
  * round's deltas.  Returns the number of rounds in *rounds. */
-int orc_pr(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
+int orc_pr(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride,
            double init, double acc, double damping, uint32_t max_rounds,
            double *value, uint32_t *rounds) {
   double *delta = (double *)malloc(sizeof(double) * (size_t)n);
@@ -210,12 +213,12 @@ int orc_pr(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
       double d = delta[v];
       value[v] += d;
       delta[v] = 0.0;
-      uint32_t deg = np[v + 1] - np[v];
+      uint32_t deg = (uint32_t)(np[v + 1] - np[v]);
       push[v] = deg ? damping * d / (double)deg : 0.0;
     }
     for (size_t k = 0; k < na; ++k) {
       uint32_t v = act[k];
-      for (uint32_t i = np[v]; i < np[v + 1]; ++i) delta[ed[(size_t)i * stride]] += push[v];
+      for (uint64_t i = np[v]; i < np[v + 1]; ++i) delta[ed[(size_t)i * stride]] += push[v];
     }
   }
   if (rounds) *rounds = r;
@@ -308,7 +311,7 @@ static inline int cas_max(uint32_t *p, uint32_t v) {
 /* Frontier-driven label correction shared by BFS/SSSP/SSWP/CC: each round
  * relaxes the out-edges of the vertices changed in the previous round
  * (algo 0 bfs, 1 sssp, 2 sswp, 3 cc), until no value changes. */
-static int omp_frontier(int algo, uint32_t n, const uint32_t *np, const uint32_t *ed,
+static int omp_frontier(int algo, uint32_t n, const uint64_t *np, const uint32_t *ed,
                         uint32_t stride, uint32_t src, uint32_t *val, uint32_t *rounds_out) {
   uint32_t *front = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
   uint32_t *next = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
@@ -339,7 +342,7 @@ static int omp_frontier(int algo, uint32_t n, const uint32_t *np, const uint32_t
       for (int64_t k = 0; k < (int64_t)nf; ++k) {
         uint32_t u = front[k];
         uint32_t du = __atomic_load_n(&val[u], __ATOMIC_RELAXED);
-        for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+        for (uint64_t i = np[u]; i < np[u + 1]; ++i) {
           uint32_t v = ed[(size_t)i * stride];
           uint32_t c;
           int upd;
@@ -376,7 +379,7 @@ static int omp_frontier(int algo, uint32_t n, const uint32_t *np, const uint32_t
   return 0;
 }
 
-int omp_bfs(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
+int omp_bfs(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
   return omp_frontier(0, n, np, ed, stride, src, out, 0);
 }
 /* Appends v to a shared array through a thread-local block of 1024. */
@@ -405,7 +408,7 @@ static inline void tl_flush(tl_buf *b, uint32_t *out, size_t *cnt) {
  * bucket is taken.  Every vertex whose distance changes has its out-edges
  * relaxed afterwards, so the result is the exact fixpoint (the same labels as
  * orc_sssp); the buckets only cut repeated relaxations. */
-static int omp_delta_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t src,
+static int omp_delta_sssp(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t src,
                           uint32_t delta, uint32_t *val) {
   uint32_t *front = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
   uint32_t *next = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
@@ -434,7 +437,7 @@ static int omp_delta_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, ui
         for (int64_t k = 0; k < (int64_t)nf; ++k) {
           const uint32_t u = front[k];
           const uint32_t du = __atomic_load_n(&val[u], __ATOMIC_RELAXED);
-          for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+          for (uint64_t i = np[u]; i < np[u + 1]; ++i) {
             const uint32_t v = ed[2 * (size_t)i];
             const uint32_t c = du + ed[2 * (size_t)i + 1];
             if (!cas_min(&val[v], c)) continue;
@@ -482,14 +485,14 @@ static int omp_delta_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, ui
   return 0;
 }
 
-int omp_sssp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
+int omp_sssp(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
   if (stride != 2) return -2;
   return omp_delta_sssp(n, np, ed, src, 32, out);
 }
 
 /* Frontier form of omp_sssp (Bellman-Ford rounds without buckets), kept as a
  * second exact method for the tests. */
-int omp_sssp_frontier(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t src,
+int omp_sssp_frontier(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride, uint32_t src,
                       uint32_t *out) {
   if (stride != 2) return -2;
   return omp_frontier(1, n, np, ed, stride, src, out, 0);
@@ -500,7 +503,7 @@ int omp_sssp_frontier(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32
  * SSWP), by one bit-parallel search: every vertex carries a 64-bit mask of the
  * sources that reach it, and a vertex whose mask gains bits pushes them along
  * its out-edges in the next round. */
-int omp_reach_multi(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t nsrc,
+int omp_reach_multi(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride, uint32_t nsrc,
                     const uint32_t *src, uint64_t *reached) {
   if (nsrc == 0 || nsrc > 64) return -2;
   uint64_t *mask = (uint64_t *)calloc(n, sizeof(uint64_t));
@@ -523,7 +526,7 @@ int omp_reach_multi(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t
       for (int64_t k = 0; k < (int64_t)nf; ++k) {
         const uint32_t u = front[k];
         const uint64_t mu = __atomic_load_n(&mask[u], __ATOMIC_RELAXED);
-        for (uint32_t i = np[u]; i < np[u + 1]; ++i) {
+        for (uint64_t i = np[u]; i < np[u + 1]; ++i) {
           const uint32_t v = ed[(size_t)i * stride];
           const uint64_t mv = __atomic_load_n(&mask[v], __ATOMIC_RELAXED);
           if ((mu & ~mv) == 0) continue;
@@ -559,16 +562,16 @@ int omp_reach_multi(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t
   free(mask); free(front); free(next); free(inq);
   return 0;
 }
-int omp_sswp(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
+int omp_sswp(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride, uint32_t src, uint32_t *out) {
   if (stride != 2) return -2;
   return omp_frontier(2, n, np, ed, stride, src, out, 0);
 }
-int omp_cc(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, uint32_t *out) {
+int omp_cc(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride, uint32_t *out) {
   return omp_frontier(3, n, np, ed, stride, 0, out, 0);
 }
 
 /* Same rounds as orc_pr, in parallel (atomic double adds). */
-int omp_pr(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, double init,
+int omp_pr(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride, double init,
            double acc, double damping, uint32_t max_rounds, double *value, uint32_t *rounds) {
   double *delta = (double *)malloc(sizeof(double) * (size_t)n);
   double *push = (double *)malloc(sizeof(double) * (size_t)n);
@@ -584,7 +587,7 @@ int omp_pr(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, 
       if (d > acc) {
         value[v] += d;
         delta[v] = 0.0;
-        uint32_t deg = np[v + 1] - np[v];
+        uint32_t deg = (uint32_t)(np[v + 1] - np[v]);
         push[v] = deg ? damping * d / (double)deg : 0.0;
         ++na;
       } else {
@@ -596,7 +599,7 @@ int omp_pr(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride, 
     for (int64_t v = 0; v < (int64_t)n; ++v) {
       double p = push[v];
       if (p == 0.0) continue;
-      for (uint32_t i = np[v]; i < np[v + 1]; ++i) {
+      for (uint64_t i = np[v]; i < np[v + 1]; ++i) {
         double *t = &delta[ed[(size_t)i * stride]];
 #pragma omp atomic
         *t += p;
@@ -783,7 +786,7 @@ static uint32_t uf_root(uint32_t *par, uint32_t x) {
 /* count sources (may repeat only when count exceeds the candidates), picked
  * uniformly among the out-degree > 0 vertices of the largest weakly
  * connected component (ties: the component with the smallest id). */
-int orc_pick_sources(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_t stride,
+int orc_pick_sources(uint32_t n, const uint64_t *np, const uint32_t *ed, uint32_t stride,
                      uint32_t count, uint64_t seed, uint32_t *out) {
   uint32_t *par = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
   uint32_t *size = (uint32_t *)calloc(n, sizeof(uint32_t));
@@ -792,7 +795,7 @@ int orc_pick_sources(uint32_t n, const uint32_t *np, const uint32_t *ed, uint32_
   for (int64_t v = 0; v < (int64_t)n; ++v) par[v] = (uint32_t)v;
 #pragma omp parallel for schedule(dynamic, 4096)
   for (int64_t v = 0; v < (int64_t)n; ++v) {
-    for (uint32_t i = np[v]; i < np[v + 1]; ++i) {
+    for (uint64_t i = np[v]; i < np[v + 1]; ++i) {
       uint32_t x = (uint32_t)v, y = ed[(size_t)i * stride];
       for (;;) {
         x = uf_root(par, x);

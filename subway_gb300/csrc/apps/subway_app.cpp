@@ -15,7 +15,8 @@
 // reference writes 6, 9 round-trips every float exactly).
 //
 // Invoked as `converter`, it is the reference's tools/converter: one argument,
-// a .el or .wel file, written beside it as .bcsr or .bwcsr
+// a .el or .wel file, written beside it as .bcsr or .bwcsr (.bcsr64 / .bwcsr64
+// at 2^32 edges or more)
 // (tools/converter.cpp:20-172), through the library's parallel text reader.
 
 #include <stdio.h>
@@ -152,7 +153,13 @@ int convert(int argc, char **argv) {
   sgw_graph *g = nullptr;
   int st = sgw_graph_load(in.c_str(), &g);
   if (st != SGW_OK) die(st, "converter");
-  std::string outp = in.substr(0, dot + 1) + (ext == "el" ? "bcsr" : "bwcsr");
+  // 2^32 edges or more do not fit the u32 header: the 64-bit form instead
+  uint32_t n = 0;
+  uint64_t m = 0;
+  sgw_graph_info64(g, &n, &m, nullptr);
+  std::string outp = in.substr(0, dot + 1) + (ext == "el" ? "bcsr" : "bwcsr") +
+                     (m >= (uint64_t(1) << 32) ? "64" : "");
+  if (m >= (uint64_t(1) << 32)) printf("%llu edges: writing %s\n", (unsigned long long)m, outp.c_str());
   st = sgw_graph_save(g, outp.c_str());
   sgw_graph_free(g);
   if (st != SGW_OK) die(st, "converter");
@@ -185,13 +192,14 @@ int main(int argc, char **argv) {
   // text files parsed
   const size_t dot = a.input.find_last_of('.');
   const std::string ext = dot == std::string::npos ? "" : a.input.substr(dot + 1);
-  int st = (ext == "bcsr" || ext == "bwcsr") ? sgw_graph_map(a.input.c_str(), &g)
-                                             : sgw_graph_load(a.input.c_str(), &g);
+  const bool binary = ext == "bcsr" || ext == "bwcsr" || ext == "bcsr64" || ext == "bwcsr64";
+  int st = binary ? sgw_graph_map(a.input.c_str(), &g) : sgw_graph_load(a.input.c_str(), &g);
   if (st != SGW_OK) die(st, "ReadGraph");
-  uint32_t n = 0, m = 0;
+  uint32_t n = 0;
+  uint64_t m = 0;
   int weighted = 0;
-  sgw_graph_info(g, &n, &m, &weighted);
-  printf("Done reading.\nNumber of nodes = %u\nNumber of edges = %u\n", n, m);
+  sgw_graph_info64(g, &n, &m, &weighted);
+  printf("Done reading.\nNumber of nodes = %u\nNumber of edges = %llu\n", n, (unsigned long long)m);
   printf("Graph Reading finished in %g (s).\n", (now_ms() - t0) / 1000.0);
 
   sgw_engine_opts o;

@@ -42,9 +42,9 @@ constexpr uint32_t kBUnroll = 4;
 
 struct BItem {
   uint32_t u;    // source vertex
-  uint32_t e0;   // first edge
+  uint32_t e0;   // first edge: low 32 bits
   uint32_t cnt;  // edges in this item
-  uint32_t pad;
+  uint32_t e0hi; //   and high 32 bits
 };
 
 // counters: [0] work items, [1] frontier vertices, [2] iterations run,
@@ -86,13 +86,16 @@ __device__ __forceinline__ BItem b_item(const BItem *items, uint32_t i) {
   it.u = v.x;
   it.e0 = v.y;
   it.cnt = v.z;
-  it.pad = v.w;
+  it.e0hi = v.w;
   return it;
 }
 
 // Frontier phase.  ctr[0]: work items appended, ctr[1]: frontier vertices;
 // err: set to 1 when the item list overflows.
-__device__ __forceinline__ void b_frontier(uint32_t n, const uint32_t *__restrict__ off, unsigned long long *cur,
+__device__ __forceinline__ size_t b_first_edge(const BItem &it) { return ((size_t)it.e0hi << 32) | it.e0; }
+
+__device__ __forceinline__ void b_frontier(uint32_t n, const uint32_t *__restrict__ off,
+                                           const unsigned long long *__restrict__ obase, unsigned long long *cur,
                                            unsigned long long *next, BItem *items, uint32_t cap, uint32_t *ctr,
                                            uint32_t chunk, uint32_t *err) {
   const int lane = threadIdx.x & 31;
@@ -100,7 +103,8 @@ __device__ __forceinline__ void b_frontier(uint32_t n, const uint32_t *__restric
   // loop bound rounded up to whole warps so every lane reaches the shuffles
   const uint32_t limit = (n + 31) & ~31u;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < limit; v += stride) {
-    uint32_t nch = 0, deg = 0, e0 = 0;
+    uint32_t nch = 0, deg = 0;
+    unsigned long long e0 = 0;
     bool act = false;
     if (v < n) {
       const unsigned long long m = __ldcg(&next[v]);
@@ -108,8 +112,8 @@ __device__ __forceinline__ void b_frontier(uint32_t n, const uint32_t *__restric
         act = true;
         cur[v] = m;
         next[v] = 0ull;
-        e0 = off[v];
-        deg = off[v + 1] - e0;
+        e0 = sgw::off_at(off, obase, v);
+        deg = off[v + 1] - off[v];
         nch = (deg + chunk - 1) / chunk;
       }
     }
@@ -130,9 +134,10 @@ __device__ __forceinline__ void b_frontier(uint32_t n, const uint32_t *__restric
       if (base + c < cap) {
         BItem it;
         it.u = v;
-        it.e0 = e0 + c * chunk;
+        const unsigned long long f = e0 + (unsigned long long)c * chunk;
+        it.e0 = (uint32_t)f;
         it.cnt = min(chunk, deg - c * chunk);
-        it.pad = 0;
+        it.e0hi = (uint32_t)(f >> 32);
         items[base + c] = it;
       } else {
         atomicExch(err, 1u);
@@ -142,10 +147,11 @@ __device__ __forceinline__ void b_frontier(uint32_t n, const uint32_t *__restric
 }
 
 __global__ void __launch_bounds__(kBThreads) k_b_frontier(uint32_t n, const uint32_t *__restrict__ off,
+                                                          const unsigned long long *__restrict__ obase,
                                                           unsigned long long *cur, unsigned long long *next,
                                                           BItem *items, uint32_t cap, uint32_t *ctr,
                                                           uint32_t chunk) {
-  b_frontier(n, off, cur, next, items, cap, ctr, chunk, &ctr[3]);
+  b_frontier(n, off, obase, cur, next, items, cap, ctr, chunk, &ctr[3]);
 }
 
 // Distance-lane relaxation phase over the nitems work items.
@@ -170,7 +176,7 @@ __device__ __forceinline__ void b_relax(const BItem *items, uint32_t nitems,
         // lane k loads edge c + k; the warp then walks them together
         uint32_t rd = 0, rw = 0;
         if (c + lane < it.cnt) {
-          const size_t e = (size_t)it.e0 + c + lane;
+          const size_t e = b_first_edge(it) + c + lane;
           if (W == 1) {
             const uint32_t r = edges[e];
             rd = r & dmask;
@@ -244,7 +250,7 @@ __device__ __forceinline__ void b_bfs_relax(const BItem *items, uint32_t nitems,
     const unsigned long long f = __ldcg(&cur[it.u]);
     if (f == 0ull) continue;
     for (uint32_t c = lane; c < it.cnt; c += 32) {
-      const size_t e = (size_t)it.e0 + c;
+      const size_t e = b_first_edge(it) + c;
       const uint32_t dst = W == 1 ? (edges[e] & dmask) : edges[2 * e];
       if ((__ldcg(&seen[dst]) & f) == f) continue;  // every query here has been there (a stale read only costs the atomic)
       const unsigned long long fresh = f & ~atomicOr(&seen[dst], f);
@@ -278,6 +284,7 @@ struct BPersist {
   uint32_t n, cap, chunk, pbits, max_iters, expect_blocks;
   unsigned long long wait_ns;
   const uint32_t *off, *edges;
+  const unsigned long long *obase;
   uint32_t *dist, *ctr;
   unsigned long long *cur, *next, *seen;
   BItem *items;
@@ -325,7 +332,7 @@ template <bool SSSP, int W, int L>
 __global__ void __launch_bounds__(kBThreads) k_b_persist(BPersist a) {
   for (uint32_t it = 0;; ++it) {
     uint32_t *c = a.ctr + 4 + 2 * (it & 1u);
-    b_frontier(a.n, a.off, a.cur, a.next, a.items, a.cap, c, a.chunk, a.ctr + 3);
+    b_frontier(a.n, a.off, a.obase, a.cur, a.next, a.items, a.cap, c, a.chunk, a.ctr + 3);
     if (!b_grid_sync(a)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       uint32_t *cn = a.ctr + 4 + 2 * ((it + 1) & 1u);
@@ -405,13 +412,15 @@ struct sgw_batch {
   const sgw_graph *g = nullptr;
   int device = 0;
   int num_sms = 0;
-  uint32_t n = 0, m = 0, W = 1, pbits = 0;
+  uint32_t n = 0, W = 1, pbits = 0;
+  uint64_t m = 0;
   uint32_t lanes = 64;            // 32 or 64 distance columns
   uint32_t chunk = 256;           // edges per work item
   uint32_t items_cap = 0;
   char *d_arena = nullptr;
   size_t arena_bytes = 0;
   uint32_t *d_off = nullptr, *d_edges = nullptr, *d_dist = nullptr, *d_stage = nullptr;
+  unsigned long long *d_obase = nullptr;  // u64 node pointers: full pointer of every 1024th vertex
   unsigned long long *d_cur = nullptr, *d_next = nullptr, *d_seen = nullptr;
   BItem *d_items = nullptr;
   uint32_t *d_ctr = nullptr, *d_src = nullptr;
@@ -435,7 +444,7 @@ int capture_body(sgw_batch *b, cudaGraph_t body, cudaGraphConditionalHandle h) {
   CK(cudaStreamBeginCaptureToGraph(b->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   k_b_reset<<<1, 1, 0, b->s>>>(b->d_ctr);
   const uint32_t grid = (uint32_t)b->num_sms * 8;
-  k_b_frontier<<<grid, kBThreads, 0, b->s>>>(b->n, b->d_off, b->d_cur, b->d_next, b->d_items, b->items_cap,
+  k_b_frontier<<<grid, kBThreads, 0, b->s>>>(b->n, b->d_off, b->d_obase, b->d_cur, b->d_next, b->d_items, b->items_cap,
                                              b->d_ctr, b->chunk);
   if (SSSP)
     k_b_relax<SSSP, W, L><<<grid, kBThreads, 0, b->s>>>(b->d_items, b->d_ctr, b->items_cap, b->d_edges, b->pbits,
@@ -495,6 +504,7 @@ int launch_persist_t(sgw_batch *b, uint32_t extra_blocks, unsigned long long wai
   a.expect_blocks = grid + extra_blocks;
   a.wait_ns = wait_ns;
   a.off = b->d_off;
+  a.obase = b->d_obase;
   a.edges = b->d_edges;
   a.dist = b->d_dist;
   a.ctr = b->d_ctr;
@@ -592,7 +602,9 @@ int sgw_batch_create(const sgw_graph *g, const sgw_engine_opts *opts, uint32_t l
   }
   b->items_cap = (uint32_t)std::min<uint64_t>((uint64_t)g->m / b->chunk + g->n + 64, 0xffffffffull);
   b->stage_vertices = std::min<uint32_t>(g->n, 1u << 22);
-  const size_t need = al(4ull * (g->n + 1)) + al((size_t)g->m * 4 * b->W) + al((size_t)g->n * lanes * 4) +
+  const bool wide = g->node_pointer64 != nullptr;
+  const size_t nbase = (g->n >> sgw::kOffGroupLog2) + 2;
+  const size_t need = al(4ull * (g->n + 1)) + (wide ? al(8 * nbase) : 0) + al((size_t)g->m * 4 * b->W) + al((size_t)g->n * lanes * 4) +
                       3 * al(8ull * g->n) + al(sizeof(BItem) * (size_t)b->items_cap) + al(64) + al(256) +
                       al((size_t)b->stage_vertices * lanes * 4);
   if (o.budget_bytes && need > o.budget_bytes) {
@@ -607,6 +619,7 @@ int sgw_batch_create(const sgw_graph *g, const sgw_engine_opts *opts, uint32_t l
   char *p = b->d_arena;
   auto take = [&](size_t bytes) { char *r = p; p += al(bytes); return r; };
   b->d_off = (uint32_t *)take(4ull * (g->n + 1));
+  if (wide) b->d_obase = (unsigned long long *)take(8 * nbase);
   b->d_edges = (uint32_t *)take((size_t)g->m * 4 * b->W);
   b->d_dist = (uint32_t *)take((size_t)g->n * lanes * 4);
   b->d_cur = (unsigned long long *)take(8ull * g->n);
@@ -622,7 +635,17 @@ int sgw_batch_create(const sgw_graph *g, const sgw_engine_opts *opts, uint32_t l
       cudaMallocHost(&b->h_ctr, 64) != cudaSuccess ||
       cudaHostAlloc((void **)&b->h_out, (size_t)g->n * lanes * 4, cudaHostAllocPortable) != cudaSuccess)
     return cleanup(sgw::fail(SGW_ECUDA, "stream/event/pinned setup"));
-  cudaError_t ce = cudaMemcpyAsync(b->d_off, g->node_pointer, 4ull * (g->n + 1), cudaMemcpyHostToDevice, b->s);
+  cudaError_t ce;
+  if (!wide) {
+    ce = cudaMemcpyAsync(b->d_off, g->node_pointer, 4ull * (g->n + 1), cudaMemcpyHostToDevice, b->s);
+  } else {
+    std::vector<uint32_t> lo((size_t)g->n + 1);
+    std::vector<unsigned long long> base(nbase);
+    if (!sgw::device_offsets(g, lo.data(), base.data()))
+      return cleanup(sgw::fail(SGW_ERANGE, "1024 consecutive vertices hold 2^32 edges or more"));
+    ce = cudaMemcpy(b->d_off, lo.data(), 4 * lo.size(), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(b->d_obase, base.data(), 8 * base.size(), cudaMemcpyHostToDevice);
+  }
   if (ce == cudaSuccess && g->m)
     ce = cudaMemcpyAsync(b->d_edges, src_edges, (size_t)g->m * 4 * b->W, cudaMemcpyHostToDevice, b->s);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->s);

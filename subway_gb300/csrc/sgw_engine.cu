@@ -67,12 +67,16 @@ struct sgw_engine {
   int num_sms = 0;
   sgw_engine_opts opts{};
   uint64_t budget = 0;
-  uint32_t n = 0, m = 0, W = 1;  // W: u32 words per edge record
+  uint32_t n = 0, W = 1;  // W: u32 words per edge record
+  uint64_t m = 0;
 
   // device arena
   char *d_arena = nullptr;
   size_t arena_bytes = 0;
-  uint32_t *d_off = nullptr;
+  uint32_t *d_off = nullptr;               // node pointers (their low 32 bits when wide)
+  unsigned long long *d_obase = nullptr;   // wide: node pointer of every 1024th vertex
+  bool wide = false;                       // u64 node pointers on the host
+  uint32_t edge_limit = 0;                 // most edges one generate queues (0: no limit)
   uint32_t *d_value = nullptr;
   uint8_t *d_l1 = nullptr, *d_l2 = nullptr;
   uint32_t range_inner_cap = 0;  // learned policy: inner-iteration cap of the running range
@@ -115,7 +119,7 @@ struct sgw_engine {
 
   bool vec_gather = false;                 // host records readable as aligned 16-B words
   uint32_t cur_streamed = 0;               // partition being relaxed: whole-range buffer
-  uint32_t cur_stream_base = 0;            //   and the first edge of that range
+  uint64_t cur_stream_base = 0;            //   and the first edge of that range
   uint32_t pbits = 0;                      // packed: bits of the destination id
   cudaStream_t s_comp = nullptr, s_copy = nullptr;
   cudaEvent_t ev_ready[kMaxBuf] = {}, ev_free[kMaxBuf] = {};
@@ -364,19 +368,20 @@ int read_ctl(sgw_engine *e) {
 enum Family { FAM_INT = 0, FAM_PR = 1 };
 
 struct Layout {
-  size_t off, tflag, tagg, tincl, ctl, mlp, sel, gmask, hct;  // common
+  size_t off, obase, tflag, tagg, tincl, ctl, mlp, sel, gmask, hct;  // common
   size_t value, l1, l2, queue, ptr, delta, qpush;     // family
   size_t parts, ranges, rstat, wl, buf[kMaxBuf], total;
   uint64_t cap;
   uint32_t max_parts, wl_cap;
 };
 
-Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
+Layout make_layout(int fam, uint32_t n, uint64_t m, uint32_t esz, uint32_t nbuf,
                    uint32_t num_tiles, uint64_t cap, uint32_t chunk, uint32_t tdm) {
   Layout L{};
   size_t p = 0;
   auto take = [&](size_t bytes) { size_t at = p; p += align_up(bytes, 256); return at; };
   L.off = take(4ull * (n + 1));
+  L.obase = take(8ull * ((n >> kOffGroupLog2) + 2));
   L.tflag = take(4ull * num_tiles);
   L.tagg = take(8ull * num_tiles);
   L.tincl = take(8ull * num_tiles);
@@ -410,7 +415,7 @@ Layout make_layout(int fam, uint32_t n, uint32_t m, uint32_t esz, uint32_t nbuf,
 }
 
 // Largest edge-buffer capacity whose layout fits `bytes` (0 if none does).
-uint64_t fit_cap(int fam, const sgw_engine_opts &o, uint32_t n, uint32_t m, uint32_t esz,
+uint64_t fit_cap(int fam, const sgw_engine_opts &o, uint32_t n, uint64_t m, uint32_t esz,
                  uint32_t nbuf, uint32_t num_tiles, uint64_t bytes) {
   auto total = [&](uint64_t cap) {
     return (uint64_t)make_layout(fam, n, m, esz, nbuf, num_tiles, cap, o.chunk_edges, o.tile_degree_max).total;
@@ -440,6 +445,7 @@ int carve(sgw_engine *e, int fam, uint64_t cap) {
   if (L.total > e->arena_bytes) return fail(SGW_EBUDGET, "layout exceeds the arena");
   char *b = e->d_arena;
   e->d_off = (uint32_t *)(b + L.off);
+  e->d_obase = (unsigned long long *)(b + L.obase);
   e->d_tflag = (uint32_t *)(b + L.tflag);
   e->d_tagg = (unsigned long long *)(b + L.tagg);
   e->d_tincl = (unsigned long long *)(b + L.tincl);
@@ -472,17 +478,17 @@ int carve(sgw_engine *e, int fam, uint64_t cap) {
   // static vertex ranges: greedy runs of whole vertices whose edges fit one
   // buffer; a vertex above the buffer is a range of its own
   e->ranges.clear();
-  const uint32_t *np = e->g->node_pointer;
+  const sgw_graph *g = e->g;
   for (uint32_t v = 0; v < e->n;) {
-    const uint64_t limit = (uint64_t)np[v] + e->cap;
+    const uint64_t limit = np_at(g, v) + e->cap;
     uint32_t lo = v + 1, hi = e->n + 1;  // first index in (v, n] with np > limit
     while (lo < hi) {
       const uint32_t mid = lo + (hi - lo) / 2;
-      if ((uint64_t)np[mid] <= limit) lo = mid + 1; else hi = mid;
+      if (np_at(g, mid) <= limit) lo = mid + 1; else hi = mid;
     }
     uint32_t v1 = lo - 1;
     if (v1 <= v) v1 = v + 1;
-    e->ranges.push_back(RangeInfo{v, v1, np[v], np[v1]});
+    e->ranges.push_back(RangeInfo{v, v1, np_at(g, v), np_at(g, v1)});
     v = v1;
   }
   if (e->ranges.size() > e->max_parts) return fail(SGW_ERANGE, "too many vertex ranges");
@@ -558,6 +564,7 @@ int launch_generate(sgw_engine *e, int consume) {
   a.epoch = e->epoch;
   a.num_tiles = e->num_tiles;
   a.consume = consume;
+  a.edge_limit = e->fam == FAM_INT ? e->edge_limit : 0u;
   a.delta = e->d_delta;
   a.pval = e->d_pval;
   a.qpush = e->d_qpush;
@@ -657,6 +664,45 @@ int enqueue_gather(sgw_engine *e, uint32_t p, cudaStream_t s) {
   return gather_into(e, q, p % e->nbuf, s);
 }
 
+// Opts the vectorised gather kernels into more than 48 KB of dynamic shared
+// memory where their tile needs it.
+template <bool WIDE>
+bool allow_gather_smem(size_t bytes) {
+  if (bytes <= 48 * 1024) return true;
+  const auto A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  return cudaFuncSetAttribute(k_gather_v<4, true, WIDE>, A, (int)bytes) == cudaSuccess &&
+         cudaFuncSetAttribute(k_gather_v<4, false, WIDE>, A, (int)bytes) == cudaSuccess &&
+         cudaFuncSetAttribute(k_gather_v<8, false, WIDE>, A, (int)bytes) == cudaSuccess;
+}
+
+// The gather kernel for the engine's transfer form; WIDE: host positions
+// of 2^32 records or more (u64 node pointers).
+template <bool WIDE>
+void launch_gather(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s, uint32_t grid,
+                   const HostChunks &h16, const HostChunks &hw16) {
+  const unsigned long long *ob = WIDE ? e->d_obase : nullptr;
+  const size_t smem = WIDE ? kGatherSmemBytesWide : kGatherSmemBytes;
+  const uint32_t cnt = (uint32_t)q.edge_count;
+  if (e->vec_gather && e->W == 1 && e->use_w)  // split form: destination words and weight bytes
+    k_gather_v<4, true, WIDE><<<grid, kGatherThreads, smem, s>>>(e->d_queue, e->d_ptr, e->d_off, ob, h16,
+                                                                 e->d_buf[b], hw16, e->d_wbuf[b], q.from, q.size,
+                                                                 q.edge_from, cnt);
+  else if (e->vec_gather && e->W == 1)
+    k_gather_v<4, false, WIDE><<<grid, kGatherThreads, smem, s>>>(e->d_queue, e->d_ptr, e->d_off, ob, h16,
+                                                                  e->d_buf[b], hw16, nullptr, q.from, q.size,
+                                                                  q.edge_from, cnt);
+  else if (e->vec_gather)
+    k_gather_v<8, false, WIDE><<<grid, kGatherThreads, smem, s>>>(e->d_queue, e->d_ptr, e->d_off, ob, h16,
+                                                                  e->d_buf[b], hw16, nullptr, q.from, q.size,
+                                                                  q.edge_from, cnt);
+  else if (e->W == 1)
+    k_gather<1, WIDE><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, ob, h16, e->d_buf[b],
+                                                      q.from, q.size, q.edge_from, cnt);
+  else
+    k_gather<2, WIDE><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, ob, h16, e->d_buf[b],
+                                                      q.from, q.size, q.edge_from, cnt);
+}
+
 // Gathers partition q's active edges into buffer b on stream s, after the
 // buffer's last reader, and records ev_ready[b].
 int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
@@ -673,24 +719,8 @@ int gather_into(sgw_engine *e, const Part &q, uint32_t b, cudaStream_t s) {
   const uint32_t grid = std::min<uint32_t>(grid_for(e, q.edge_count, kGatherTile), gmax);
   const HostChunks h16{e->d_hct, e->hs_ends.shift};
   const HostChunks hw16{e->d_hct + kMaxHostChunks, e->hs_w.shift};
-  if (e->vec_gather && e->W == 1 && e->use_w)  // split form: destination words and weight bytes
-    k_gather_v<4, true><<<grid, kGatherThreads, kGatherSmemBytes, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
-                                                        hw16, e->d_wbuf[b], q.from, q.size,
-                                                        q.edge_from, (uint32_t)q.edge_count);
-  else if (e->vec_gather && e->W == 1)
-    k_gather_v<4, false><<<grid, kGatherThreads, kGatherSmemBytes, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
-                                                         hw16, nullptr, q.from, q.size, q.edge_from,
-                                                         (uint32_t)q.edge_count);
-  else if (e->vec_gather)
-    k_gather_v<8, false><<<grid, kGatherThreads, kGatherSmemBytes, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b],
-                                                         hw16, nullptr, q.from, q.size, q.edge_from,
-                                                         (uint32_t)q.edge_count);
-  else if (e->W == 1)
-    k_gather<1><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b], q.from,
-                                                q.size, q.edge_from, (uint32_t)q.edge_count);
-  else
-    k_gather<2><<<grid, kGatherThreads, 0, s>>>(e->d_queue, e->d_ptr, e->d_off, h16, e->d_buf[b], q.from,
-                                                q.size, q.edge_from, (uint32_t)q.edge_count);
+  if (e->wide) launch_gather<true>(e, q, b, s, grid, h16, hw16);
+  else launch_gather<false>(e, q, b, s, grid, h16, hw16);
   CK(cudaGetLastError());
   e->stats.h2d_bytes += q.edge_count * (4ull * e->W + (e->use_w ? 1 : 0));
   e->stats.gather_bytes += q.edge_count * (4ull * e->W + (e->use_w ? 1 : 0));
@@ -722,7 +752,7 @@ int launch_relax_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter, u
   a.chunk_edges = e->opts.chunk_edges;
   a.pbits = e->pbits;
   a.streamed = e->cur_streamed;
-  a.stream_base = e->cur_stream_base;
+  a.stream_base = (uint32_t)e->cur_stream_base;  // with the low words of off: offsets mod 2^32
   a.off = e->d_off;
   a.wbuf = e->use_w ? e->d_wbuf[b] : nullptr;
   const uint32_t g1 = grid_for(e, q.size, kRelaxThreads);
@@ -770,7 +800,7 @@ int launch_pr_pair(sgw_engine *e, const Part &q, uint32_t b, uint32_t iter) {
   a.chunk_edges = e->opts.chunk_edges;
   a.pbits = e->pbits;
   a.streamed = e->cur_streamed;
-  a.stream_base = e->cur_stream_base;
+  a.stream_base = (uint32_t)e->cur_stream_base;  // with the low words of off: offsets mod 2^32
   a.off = e->d_off;
   a.acc = (double)e->params.pr_acc;
   a.damping = (double)e->params.pr_damping;
@@ -822,7 +852,7 @@ int process_hub(sgw_engine *e, const Part &q, uint32_t b) {
   else k_hub_claim<false><<<1, 1, 0, e->s_comp>>>(u, e->d_value, e->d_l1, e->d_l2, e->d_ctl);
   CK(cudaGetLastError());
   const uint64_t deg = q.edge_count;
-  const uint64_t hoff = e->g->node_pointer[u];
+  const uint64_t hoff = np_at(e->g, u);
   const size_t esz = 4ull * e->W;
   for (uint64_t s = 0; s < deg; s += e->cap) {
     const uint32_t cnt = (uint32_t)std::min<uint64_t>(e->cap, deg - s);
@@ -916,6 +946,8 @@ int validate_params(const sgw_engine *e, const sgw_run_params *p) {
     return fail(SGW_EBUDGET, "budget too small for the PageRank vertex state (f64 ranks and residuals)");
   if (p->algo == SGW_PR && !(p->pr_acc > 0.0f) )
     return fail(SGW_EINVAL, "pr_acc must be positive");
+  if (p->algo == SGW_PR && e->m >= (uint64_t(1) << 32))  // its generate has no edge limit
+    return fail(SGW_ERANGE, "PageRank needs fewer than 2^32 edges");
   if ((p->algo == SGW_SSSP || p->algo == SGW_SSWP) && !e->g->weighted)
     return fail(SGW_EINVAL, "SSSP/SSWP need a weighted graph (.bwcsr/.wel)");
   if (p->algo != SGW_CC && p->algo != SGW_PR && p->source >= e->n)
@@ -1343,6 +1375,28 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   e->n = g->n;
   e->m = g->m;
   e->W = g->weighted ? 2 : 1;
+  e->wide = g->node_pointer64 != nullptr;
+  {
+    // queue positions are u32: at 2^32 edges and more a generate queues at
+    // most 2^31 edges, whole tiles of fewer than 2^31 edges each
+    const bool big = g->m >= (uint64_t(1) << 32);
+    uint64_t lim = o.generate_edge_limit ? o.generate_edge_limit : (big ? uint64_t(1) << 31 : 0);
+    if (big) lim = std::min<uint64_t>(lim, uint64_t(1) << 31);
+    e->edge_limit = (uint32_t)lim;
+    const uint32_t n = g->n;
+    int over = 0;
+    if (big) {
+#pragma omp parallel for reduction(| : over)
+      for (int64_t t = 0; t < (int64_t)((n + kGenTile - 1) / kGenTile); ++t) {
+        const uint64_t v0 = (uint64_t)t * kGenTile, v1 = std::min<uint64_t>(n, v0 + kGenTile);
+        if (np_at(g, v1) - np_at(g, v0) >= (uint64_t(1) << 31)) over |= 1;
+      }
+    }
+    if (over) {
+      delete e;
+      return fail(SGW_ERANGE, "a 4096-vertex tile holds 2^31 edges or more");
+    }
+  }
   // weighted records travel as one packed word when (w << bits(n)) | dst fits
   const uint32_t wmax = max_weight(g);  // one pass over the records
   bool pack = g->weighted && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SPLIT_WEIGHTS)) &&
@@ -1466,15 +1520,9 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
     if (ce != cudaSuccess) return cleanup(fail(SGW_ECUDA, "chunk table upload: %s", cudaGetErrorString(ce)));
   }
   e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && !e->hs_ends.h.empty();
-  if (kGatherSmemBytes > 48 * 1024 &&
-      (cudaFuncSetAttribute(k_gather_v<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)kGatherSmemBytes) != cudaSuccess ||
-       cudaFuncSetAttribute(k_gather_v<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)kGatherSmemBytes) != cudaSuccess ||
-       cudaFuncSetAttribute(k_gather_v<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)kGatherSmemBytes) != cudaSuccess)) {
+  if (!allow_gather_smem<false>(kGatherSmemBytes) || !allow_gather_smem<true>(kGatherSmemBytesWide)) {
     cudaGetLastError();
-    return cleanup(fail(SGW_ECUDA, "gather shared memory of %zu bytes refused", kGatherSmemBytes));
+    return cleanup(fail(SGW_ECUDA, "gather shared memory of %zu bytes refused", kGatherSmemBytesWide));
   }
   if (cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking) != cudaSuccess)
@@ -1491,7 +1539,16 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
       cudaMallocHost(&e->h_rstat, sizeof(RangeStat) * (size_t)parts_host) != cudaSuccess)
     return cleanup(fail(SGW_ECUDA, "pinned control block"));
   memset(e->h_ctl, 0, sizeof(Ctl));
-  ce = cudaMemcpyAsync(e->d_off, g->node_pointer, 4ull * (e->n + 1), cudaMemcpyHostToDevice, e->s_comp);
+  if (!e->wide) {
+    ce = cudaMemcpyAsync(e->d_off, g->node_pointer, 4ull * (e->n + 1), cudaMemcpyHostToDevice, e->s_comp);
+  } else {  // low words of every node pointer, full pointers of every group start
+    std::vector<uint32_t> lo((size_t)e->n + 1);
+    std::vector<unsigned long long> base((e->n >> kOffGroupLog2) + 2);
+    if (!device_offsets(g, lo.data(), base.data()))
+      return cleanup(fail(SGW_ERANGE, "1024 consecutive vertices hold 2^32 edges or more"));
+    ce = cudaMemcpy(e->d_off, lo.data(), 4 * lo.size(), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(e->d_obase, base.data(), 8 * base.size(), cudaMemcpyHostToDevice);
+  }
   if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_ctl, 0, sizeof(Ctl), e->s_comp);
   if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_tflag, 0, 4ull * e->num_tiles, e->s_comp);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->s_comp);

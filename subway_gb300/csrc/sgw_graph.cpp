@@ -51,26 +51,81 @@ void *host_alloc(size_t bytes, size_t *rounded) {
 void host_free(void *p) { free(p); }
 
 int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out) {
-  if (m >= (uint64_t(1) << 32))
-    return fail(SGW_ERANGE, "edge count %llu does not fit the u32 format",
-                (unsigned long long)m);
   sgw_graph *g = new (std::nothrow) sgw_graph();
   if (!g) return fail(SGW_ENOMEM, "graph object");
   g->n = n;
-  g->m = (uint32_t)m;
+  g->m = m;
   g->weighted = weighted ? 1 : 0;
   g->esz = weighted ? 8 : 4;
   g->owns = true;
-  g->node_pointer = (uint32_t *)host_alloc(sizeof(uint32_t) * (size_t(n) + 1), nullptr);
+  const bool wide = m >= (uint64_t(1) << 32);
+  void *np = host_alloc((wide ? 8 : 4) * (size_t(n) + 1), nullptr);
+  if (wide) g->node_pointer64 = (uint64_t *)np;
+  else g->node_pointer = (uint32_t *)np;
   g->edges = host_alloc(size_t(m) * g->esz, &g->edges_bytes_alloc);
-  if (!g->node_pointer || !g->edges) {
-    host_free(g->node_pointer);
+  if (!np || !g->edges) {
+    host_free(np);
     host_free(g->edges);
     delete g;
     return fail(SGW_ENOMEM, "graph arrays (n=%u m=%llu)", n, (unsigned long long)m);
   }
   *out = g;
   return SGW_OK;
+}
+
+// Sets node pointer v of a graph being built, whichever its width.
+static inline void np_set(sgw_graph *g, uint64_t v, uint64_t x) {
+  if (g->node_pointer64) g->node_pointer64[v] = x;
+  else g->node_pointer[v] = (uint32_t)x;
+}
+
+// Checks monotone node pointers (np[0] == 0, np[n] == m is the caller's) and
+// edge endpoints below n, in parallel.  Returns 0, or 1 (pointers) / 2
+// (endpoints) / 4 (an out-degree of 2^32 or more).
+static int validate_csr(const sgw_graph *g) {
+  int bad = 0;
+  const uint32_t n = g->n;
+#pragma omp parallel for reduction(| : bad)
+  for (int64_t v = 0; v < (int64_t)n; ++v) {
+    const uint64_t a = np_at(g, (uint64_t)v), b = np_at(g, (uint64_t)v + 1);
+    if (a > b) bad |= 1;
+    else if (b - a >= (uint64_t(1) << 32)) bad |= 4;
+  }
+  if (bad) return bad & 1 ? 1 : 4;
+  const uint32_t *ed = (const uint32_t *)g->edges;
+  const size_t stride = g->esz / 4;
+#pragma omp parallel for reduction(| : bad)
+  for (int64_t i = 0; i < (int64_t)g->m; ++i)
+    if (ed[size_t(i) * stride] >= n) bad |= 2;
+  return bad;
+}
+
+bool device_offsets(const sgw_graph *g, uint32_t *lo, unsigned long long *base) {
+  const uint32_t n = g->n;
+  if (!g->node_pointer64) {
+    copy_bytes(lo, g->node_pointer, 4ull * (n + 1));
+    return true;
+  }
+  const uint64_t *np = g->node_pointer64;
+  const int64_t groups = (int64_t)(n >> kOffGroupLog2) + 2;
+  int over = 0;
+#pragma omp parallel for reduction(| : over)
+  for (int64_t k = 0; k < groups; ++k) {
+    const uint64_t v0 = std::min<uint64_t>(n, (uint64_t)k << kOffGroupLog2);
+    const uint64_t v1 = std::min<uint64_t>(n, v0 + (1u << kOffGroupLog2));
+    if (np[v1] - np[v0] >= (uint64_t(1) << 32)) over = 1;
+  }
+  if (over) return false;
+#pragma omp parallel for
+  for (int64_t k = 0; k < groups; ++k) base[k] = np[std::min<uint64_t>(n, (uint64_t)k << kOffGroupLog2)];
+#pragma omp parallel for
+  for (int64_t v = 0; v <= (int64_t)n; ++v) lo[v] = (uint32_t)np[v];
+  return true;
+}
+
+static const char *csr_problem(int bad) {
+  return bad & 1 ? "node pointers not monotone"
+                 : bad & 4 ? "out-degree of 2^32 or more" : "edge endpoint out of range";
 }
 
 bool pack_bits_for(const sgw_graph *g, uint32_t wmax, uint32_t *nbits) {
@@ -303,8 +358,8 @@ static int build_csr(uint32_t n, uint64_t m0, Draw draw, uint32_t drop_vertex,
   if (st != SGW_OK) { host_free(pairs); return st; }
   {
     uint64_t acc = 0;
-    for (uint32_t v = 0; v < n; ++v) { g->node_pointer[v] = (uint32_t)acc; acc += deg[v]; }
-    g->node_pointer[n] = (uint32_t)acc;
+    for (uint32_t v = 0; v < n; ++v) { np_set(g, v, acc); acc += deg[v]; }
+    np_set(g, n, acc);
   }
   // bucket b's rows start at node_pointer[first source of bucket]
 #pragma omp parallel for schedule(dynamic, 1) num_threads(T)
@@ -312,7 +367,7 @@ static int build_csr(uint32_t n, uint64_t m0, Draw draw, uint32_t drop_vertex,
     const uint64_t *p = pairs + bstart[b];
     uint64_t u = bunique[b];
     if (u == 0) continue;
-    uint64_t pos = g->node_pointer[p[0] >> 32];
+    uint64_t pos = np_at(g, p[0] >> 32);
     if (weighted) {
       uint32_t *ed = (uint32_t *)g->edges;
       for (uint64_t i = 0; i < u; ++i) {
@@ -357,55 +412,106 @@ static bool pread_parallel(int fd, char *dst, size_t bytes, off_t off) {
   return !bad;
 }
 
-static int load_binary(const char *path, int weighted, sgw_graph **out) {
+// Binary CSR files.  .bcsr / .bwcsr (graph.cu:43-51): [u32 n][u32 m]
+// [u32 nodePointer x n][edge x m], the sentinel nodePointer[n] = m implied.
+// .bcsr64 / .bwcsr64, for graphs of 2^32 edges or more: [u64 n][u64 m]
+// [u64 nodePointer x n][edge x m]; every field and the records stay 8-byte
+// aligned, so the file maps in place.  Vertex ids stay u32 in both.
+struct BinHeader {
+  uint64_t n = 0, m = 0;
+  size_t hdr = 0, npsz = 0;  // header bytes, bytes per node pointer
+};
+
+static int read_header(int fd, const char *path, bool wide_file, int weighted, BinHeader *h) {
+  struct stat sb;
+  if (fstat(fd, &sb) != 0) return fail(SGW_EIO, "cannot stat %s", path);
+  if (wide_file) {
+    uint64_t hd[2];
+    if (pread(fd, hd, sizeof(hd), 0) != (ssize_t)sizeof(hd)) return fail(SGW_EFORMAT, "%s: truncated header", path);
+    h->n = hd[0];
+    h->m = hd[1];
+    h->hdr = 16;
+    h->npsz = 8;
+  } else {
+    uint32_t hd[2];
+    if (pread(fd, hd, sizeof(hd), 0) != (ssize_t)sizeof(hd)) return fail(SGW_EFORMAT, "%s: truncated header", path);
+    h->n = hd[0];
+    h->m = hd[1];
+    h->hdr = 8;
+    h->npsz = 4;
+  }
+  if (h->n == 0) return fail(SGW_EFORMAT, "%s: zero vertices", path);
+  if (h->n >= (uint64_t(1) << 32)) return fail(SGW_EFORMAT, "%s: %llu vertices (ids are u32)", path,
+                                               (unsigned long long)h->n);
+  const uint64_t esz = weighted ? 8 : 4;
+  const unsigned long long want = h->hdr + h->npsz * h->n + h->m * esz;
+  if (h->m > (uint64_t(1) << 40) || (unsigned long long)sb.st_size != want)
+    return fail(SGW_EFORMAT, "%s: size %lld, expected %llu for n=%llu m=%llu", path, (long long)sb.st_size,
+                want, (unsigned long long)h->n, (unsigned long long)h->m);
+  return SGW_OK;
+}
+
+// Fills the graph's node pointers [0, n) from a file's array of npsz-byte
+// pointers (u32 or u64, into a u32 or u64 array) and sets [n] = m.  False
+// when a u64 pointer above m was to be narrowed to u32 (it would wrap and
+// could pass the monotonicity check).
+static bool fill_pointers(sgw_graph *g, const void *src, size_t npsz) {
+  const uint32_t n = g->n;
+  int over = 0;
+  if (npsz == 4 && g->node_pointer) {
+    copy_bytes(g->node_pointer, src, 4ull * n);
+  } else if (npsz == 8 && g->node_pointer64) {
+    copy_bytes(g->node_pointer64, src, 8ull * n);
+  } else {
+    const uint64_t m = g->m;
+#pragma omp parallel for reduction(| : over)
+    for (int64_t v = 0; v < (int64_t)n; ++v) {
+      const uint64_t x = npsz == 8 ? ((const uint64_t *)src)[v] : (uint64_t)((const uint32_t *)src)[v];
+      if (x > m) over = 1;
+      np_set(g, (uint64_t)v, x);
+    }
+  }
+  np_set(g, n, g->m);
+  return !over;
+}
+
+static int load_binary(const char *path, int weighted, bool wide_file, sgw_graph **out) {
   int fd = open(path, O_RDONLY);
   if (fd < 0) return fail(SGW_EIO, "cannot open %s", path);
-  uint32_t hdr[2];
-  struct stat sb;
-  if (pread(fd, hdr, sizeof(hdr), 0) != (ssize_t)sizeof(hdr) || fstat(fd, &sb) != 0) {
-    close(fd);
-    return fail(SGW_EFORMAT, "%s: truncated header", path);
-  }
-  uint32_t n = hdr[0], m = hdr[1];
-  if (n == 0) { close(fd); return fail(SGW_EFORMAT, "%s: zero vertices", path); }
-  const uint32_t esz = weighted ? 8 : 4;
-  long long fsz = (long long)sb.st_size;
-  long long want = 8LL + 4LL * n + (long long)m * esz;
-  if (fsz != want) {
-    close(fd);
-    return fail(SGW_EFORMAT, "%s: size %lld, expected %lld for n=%u m=%u", path,
-                fsz, want, n, m);
-  }
-  sgw_graph *g = nullptr;
-  int st = graph_alloc(n, m, weighted, &g);
+  BinHeader h;
+  int st = read_header(fd, path, wide_file, weighted, &h);
   if (st != SGW_OK) { close(fd); return st; }
-  // [u32 n][u32 m][u32 nodePointer x n][edge x m] (graph.cu:43-51); the
-  // sentinel nodePointer[n] = m is implied
-  bool ok = pread_parallel(fd, (char *)g->node_pointer, sizeof(uint32_t) * size_t(n), 8) &&
-            pread_parallel(fd, (char *)g->edges, size_t(m) * esz, 8 + 4 * (off_t)n);
+  const uint32_t n = (uint32_t)h.n;
+  const uint32_t esz = weighted ? 8 : 4;
+  sgw_graph *g = nullptr;
+  st = graph_alloc(n, h.m, weighted, &g);
+  if (st != SGW_OK) { close(fd); return st; }
+  bool ok;
+  if ((h.npsz == 8) == (g->node_pointer64 != nullptr)) {
+    ok = pread_parallel(fd, g->node_pointer64 ? (char *)g->node_pointer64 : (char *)g->node_pointer,
+                        h.npsz * size_t(n), (off_t)h.hdr);
+    np_set(g, n, h.m);
+  } else {  // a 64-bit file of fewer than 2^32 edges: u32 pointers in memory
+    char *tmp = (char *)host_alloc(h.npsz * size_t(n), nullptr);
+    ok = tmp && pread_parallel(fd, tmp, h.npsz * size_t(n), (off_t)h.hdr);
+    const bool fits = ok && fill_pointers(g, tmp, h.npsz);
+    host_free(tmp);
+    if (ok && !fits) {
+      close(fd);
+      sgw_graph_free(g);
+      return fail(SGW_EFORMAT, "%s: %s", path, csr_problem(1));
+    }
+  }
+  ok = ok && pread_parallel(fd, (char *)g->edges, size_t(h.m) * esz, (off_t)(h.hdr + h.npsz * size_t(n)));
   close(fd);
-  g->node_pointer[n] = m;
   if (!ok) {
     sgw_graph_free(g);
     return fail(SGW_EFORMAT, "%s: truncated body", path);
   }
-  // validate: monotone pointers within [0, m], endpoints < n
-  int bad = 0;
-  const uint32_t *np = g->node_pointer;
-#pragma omp parallel for reduction(| : bad)
-  for (int64_t v = 0; v < (int64_t)n; ++v)
-    if (np[v] > np[v + 1]) bad |= 1;
-  if (!bad) {
-    const uint32_t *ed = (const uint32_t *)g->edges;
-    const size_t stride = esz / 4;
-#pragma omp parallel for reduction(| : bad)
-    for (int64_t i = 0; i < (int64_t)m; ++i)
-      if (ed[size_t(i) * stride] >= n) bad |= 2;
-  }
+  const int bad = validate_csr(g);
   if (bad) {
     sgw_graph_free(g);
-    return fail(SGW_EFORMAT, "%s: %s", path,
-                (bad & 1) ? "node pointers not monotone" : "edge endpoint out of range");
+    return fail(SGW_EFORMAT, "%s: %s", path, csr_problem(bad));
   }
   *out = g;
   return SGW_OK;
@@ -474,6 +580,62 @@ static void parse_piece(const char *base, size_t lo, size_t hi, int weighted, Te
   }
 }
 
+// Node pointers (T = u32 or u64) and rows of a graph from parsed pieces:
+// degrees, an exclusive prefix in T blocks, then placement, where thread j
+// owns the sources whose rows start in its 1/T of the edge range and scans
+// every piece in file order, keeping rows stable.
+template <class P>
+static void place_text_rows(sgw_graph *g, const std::vector<TextPiece> &pcs, int T, P *np) {
+  const uint32_t n = g->n;
+  const uint64_t m = g->m;
+  const int weighted = g->weighted;
+#pragma omp parallel for num_threads(T)
+  for (int64_t v = 0; v <= (int64_t)n; ++v) np[v] = 0;
+#pragma omp parallel for schedule(static, 1) num_threads(T)
+  for (int t = 0; t < T; ++t)
+    for (uint32_t s : pcs[t].src) __atomic_fetch_add(&np[s], (P)1, __ATOMIC_RELAXED);
+  std::vector<uint64_t> block(size_t(T) + 1, 0);
+#pragma omp parallel num_threads(T)
+  {
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    const uint64_t lo = uint64_t(n) * t / nt, hi = uint64_t(n) * (t + 1) / nt;
+    uint64_t acc = 0;
+    for (uint64_t v = lo; v < hi; ++v) acc += np[v];
+    block[t + 1] = acc;
+#pragma omp barrier
+#pragma omp single
+    for (int k = 1; k <= nt; ++k) block[k] += block[k - 1];
+    uint64_t run = block[t];
+    for (uint64_t v = lo; v < hi; ++v) {
+      const P c = np[v];
+      np[v] = (P)run;
+      run += c;
+    }
+  }
+  np[n] = (P)m;
+  std::vector<P> cur(np, np + n);
+  uint32_t *ed = (uint32_t *)g->edges;
+#pragma omp parallel num_threads(T)
+  {
+    const int j = omp_get_thread_num(), nt = omp_get_num_threads();
+    const P e_lo = (P)(m * j / nt), e_hi = (P)(m * (j + 1) / nt);
+    // first vertex whose row starts at or after e_lo / e_hi
+    const uint32_t v_lo = j == 0 ? 0 : (uint32_t)(std::lower_bound(np, np + n, e_lo) - np);
+    const uint32_t v_hi = j == nt - 1 ? n : (uint32_t)(std::lower_bound(np, np + n, e_hi) - np);
+    if (v_lo < v_hi)
+      for (const TextPiece &pc : pcs) {
+        const size_t k = pc.src.size();
+        for (size_t i = 0; i < k; ++i) {
+          const uint32_t s = pc.src[i];
+          if (s < v_lo || s >= v_hi) continue;
+          const P pos = cur[s]++;
+          if (weighted) { ed[2 * size_t(pos)] = pc.dst[i]; ed[2 * size_t(pos) + 1] = pc.w[i]; }
+          else ed[pos] = pc.dst[i];
+        }
+      }
+  }
+}
+
 static int load_text(const char *path, int weighted, sgw_graph **out) {
   int fd = open(path, O_RDONLY);
   if (fd < 0) return fail(SGW_EIO, "cannot open %s", path);
@@ -525,56 +687,17 @@ static int load_text(const char *path, int weighted, sgw_graph **out) {
   sgw_graph *g = nullptr;
   int st = graph_alloc(n, m, weighted, &g);
   if (st != SGW_OK) return st;
-  uint32_t *np = g->node_pointer;
-
-  // degrees, then an exclusive prefix in T blocks
-#pragma omp parallel for num_threads(T)
-  for (int64_t v = 0; v <= (int64_t)n; ++v) np[v] = 0;
-#pragma omp parallel for schedule(static, 1) num_threads(T)
-  for (int t = 0; t < T; ++t)
-    for (uint32_t s : pcs[t].src) __atomic_fetch_add(&np[s], 1u, __ATOMIC_RELAXED);
-  std::vector<uint64_t> block(size_t(T) + 1, 0);
-#pragma omp parallel num_threads(T)
-  {
-    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
-    const uint64_t lo = uint64_t(n) * t / nt, hi = uint64_t(n) * (t + 1) / nt;
-    uint64_t acc = 0;
-    for (uint64_t v = lo; v < hi; ++v) acc += np[v];
-    block[t + 1] = acc;
-#pragma omp barrier
-#pragma omp single
-    for (int k = 1; k <= nt; ++k) block[k] += block[k - 1];
-    uint64_t run = block[t];
-    for (uint64_t v = lo; v < hi; ++v) {
-      uint32_t c = np[v];
-      np[v] = (uint32_t)run;
-      run += c;
+  if (g->node_pointer64) place_text_rows(g, pcs, T, g->node_pointer64);
+  else place_text_rows(g, pcs, T, g->node_pointer);
+  if (g->node_pointer64) {  // rows are built sorted and in range; only a degree can overflow
+    int big = 0;
+#pragma omp parallel for reduction(| : big)
+    for (int64_t v = 0; v < (int64_t)n; ++v)
+      if (g->node_pointer64[v + 1] - g->node_pointer64[v] >= (uint64_t(1) << 32)) big = 1;
+    if (big) {
+      sgw_graph_free(g);
+      return fail(SGW_EFORMAT, "%s: %s", path, csr_problem(4));
     }
-  }
-  np[n] = (uint32_t)m;
-
-  // placement: thread j owns the sources whose rows start in its 1/T of the
-  // edge range and scans every piece in file order, keeping rows stable
-  std::vector<uint32_t> cur(np, np + n);
-  uint32_t *ed = (uint32_t *)g->edges;
-#pragma omp parallel num_threads(T)
-  {
-    const int j = omp_get_thread_num(), nt = omp_get_num_threads();
-    const uint32_t e_lo = (uint32_t)(m * j / nt), e_hi = (uint32_t)(m * (j + 1) / nt);
-    // first vertex whose row starts at or after e_lo / e_hi
-    const uint32_t v_lo = j == 0 ? 0 : (uint32_t)(std::lower_bound(np, np + n, e_lo) - np);
-    const uint32_t v_hi = j == nt - 1 ? n : (uint32_t)(std::lower_bound(np, np + n, e_hi) - np);
-    if (v_lo < v_hi)
-      for (const TextPiece &pc : pcs) {
-        const size_t k = pc.src.size();
-        for (size_t i = 0; i < k; ++i) {
-          const uint32_t s = pc.src[i];
-          if (s < v_lo || s >= v_hi) continue;
-          const uint32_t pos = cur[s]++;
-          if (weighted) { ed[2 * size_t(pos)] = pc.dst[i]; ed[2 * size_t(pos) + 1] = pc.w[i]; }
-          else ed[pos] = pc.dst[i];
-        }
-      }
   }
   *out = g;
   return SGW_OK;
@@ -618,8 +741,10 @@ int sgw_graph_load(const char *path, sgw_graph **out) {
   if (!path || !out) return fail(SGW_EINVAL, "null argument");
   *out = nullptr;
   std::string ext = extension_of(path);
-  if (ext == "bcsr") return load_binary(path, 0, out);
-  if (ext == "bwcsr") return load_binary(path, 1, out);
+  if (ext == "bcsr") return load_binary(path, 0, false, out);
+  if (ext == "bwcsr") return load_binary(path, 1, false, out);
+  if (ext == "bcsr64") return load_binary(path, 0, true, out);
+  if (ext == "bwcsr64") return load_binary(path, 1, true, out);
   if (ext == "el") return load_text(path, 0, out);
   if (ext == "wel") return load_text(path, 1, out);
   return fail(SGW_EFORMAT, "The graph format is not supported: '%s'", path);
@@ -631,17 +756,6 @@ int sgw_graph_from_csr(uint32_t n, uint32_t m, const uint32_t *node_pointer,
   if (!out || !node_pointer || (m > 0 && !edges) || n == 0)
     return fail(SGW_EINVAL, "null argument or zero vertices");
   if (node_pointer[n] != m) return fail(SGW_EINVAL, "node_pointer[n] != m");
-  // the device kernels index vertex arrays by edge endpoint: validate once
-  int bad = 0;
-  for (uint32_t v = 0; v < n && !bad; ++v)
-    if (node_pointer[v] > node_pointer[v + 1]) bad = 1;
-  const uint32_t *ed = (const uint32_t *)edges;
-  const size_t stride = weighted ? 2 : 1;
-#pragma omp parallel for reduction(| : bad)
-  for (int64_t i = 0; i < (int64_t)m; ++i)
-    if (ed[size_t(i) * stride] >= n) bad |= 2;
-  if (bad)
-    return fail(SGW_EINVAL, "%s", bad & 1 ? "node_pointer not monotone" : "edge endpoint >= n");
   sgw_graph *g = new (std::nothrow) sgw_graph();
   if (!g) return fail(SGW_ENOMEM, "graph object");
   g->n = n;
@@ -651,11 +765,50 @@ int sgw_graph_from_csr(uint32_t n, uint32_t m, const uint32_t *node_pointer,
   g->node_pointer = const_cast<uint32_t *>(node_pointer);
   g->edges = const_cast<void *>(edges);
   g->owns = false;
+  // the device kernels index vertex arrays by edge endpoint: validate once
+  if (const int bad = validate_csr(g)) {
+    delete g;
+    return fail(SGW_EINVAL, "%s", bad & 1 ? "node_pointer not monotone" : "edge endpoint >= n");
+  }
+  *out = g;
+  return SGW_OK;
+}
+
+int sgw_graph_from_csr64(uint32_t n, uint64_t m, const uint64_t *node_pointer,
+                         const void *edges, int weighted, sgw_graph **out) {
+  clear_error();
+  if (!out || !node_pointer || (m > 0 && !edges) || n == 0)
+    return fail(SGW_EINVAL, "null argument or zero vertices");
+  if (node_pointer[n] != m) return fail(SGW_EINVAL, "node_pointer[n] != m");
+  sgw_graph *g = new (std::nothrow) sgw_graph();
+  if (!g) return fail(SGW_ENOMEM, "graph object");
+  g->n = n;
+  g->m = m;
+  g->weighted = weighted ? 1 : 0;
+  g->esz = weighted ? 8 : 4;
+  g->node_pointer64 = const_cast<uint64_t *>(node_pointer);
+  g->edges = const_cast<void *>(edges);
+  g->owns = false;
+  if (const int bad = validate_csr(g)) {
+    delete g;
+    return fail(SGW_EINVAL, "%s", bad & 1 ? "node_pointer not monotone"
+                                          : bad & 4 ? "out-degree of 2^32 or more" : "edge endpoint >= n");
+  }
   *out = g;
   return SGW_OK;
 }
 
 int sgw_graph_info(const sgw_graph *g, uint32_t *n, uint32_t *m, int *weighted) {
+  if (!g) return fail(SGW_EINVAL, "null graph");
+  if (g->m >= (uint64_t(1) << 32))
+    return fail(SGW_ERANGE, "%llu edges do not fit a u32 count (sgw_graph_info64)", (unsigned long long)g->m);
+  if (n) *n = g->n;
+  if (m) *m = (uint32_t)g->m;
+  if (weighted) *weighted = g->weighted;
+  return SGW_OK;
+}
+
+int sgw_graph_info64(const sgw_graph *g, uint32_t *n, uint64_t *m, int *weighted) {
   if (!g) return fail(SGW_EINVAL, "null graph");
   if (n) *n = g->n;
   if (m) *m = g->m;
@@ -664,13 +817,13 @@ int sgw_graph_info(const sgw_graph *g, uint32_t *n, uint32_t *m, int *weighted) 
 }
 
 const uint32_t *sgw_graph_node_pointer(const sgw_graph *g) { return g ? g->node_pointer : nullptr; }
+const uint64_t *sgw_graph_node_pointer64(const sgw_graph *g) { return g ? g->node_pointer64 : nullptr; }
 const void *sgw_graph_edges(const sgw_graph *g) { return g ? g->edges : nullptr; }
 
 int sgw_graph_out_degree(const sgw_graph *g, uint32_t *out_degree) {
   if (!g || !out_degree) return fail(SGW_EINVAL, "null argument");
 #pragma omp parallel for
-  for (int64_t v = 0; v < (int64_t)g->n; ++v)
-    out_degree[v] = g->node_pointer[v + 1] - g->node_pointer[v];
+  for (int64_t v = 0; v < (int64_t)g->n; ++v) out_degree[v] = deg_at(g, (uint64_t)v);
   return SGW_OK;
 }
 
@@ -678,20 +831,45 @@ int sgw_graph_save(const sgw_graph *g, const char *path) {
   clear_error();
   if (!g || !path) return fail(SGW_EINVAL, "null argument");
   std::string ext = extension_of(path);
-  bool bin = (ext == "bcsr" || ext == "bwcsr");
+  const bool bin64 = (ext == "bcsr64" || ext == "bwcsr64");
+  const bool bin = bin64 || (ext == "bcsr" || ext == "bwcsr");
   bool txt = (ext == "el" || ext == "wel");
   if (!bin && !txt) return fail(SGW_EFORMAT, "unsupported extension for %s", path);
-  bool want_w = (ext == "bwcsr" || ext == "wel");
+  bool want_w = (ext == "bwcsr" || ext == "bwcsr64" || ext == "wel");
   if (want_w && !g->weighted)
     return fail(SGW_EINVAL, "%s needs a weighted graph", path);
+  if (bin && !bin64 && g->m >= (uint64_t(1) << 32))
+    return fail(SGW_ERANGE, "%llu edges do not fit the u32 header of %s (write .%s64)",
+                (unsigned long long)g->m, path, ext.c_str());
   FILE *f = fopen(path, "wb");
   if (!f) return fail(SGW_EIO, "cannot create %s", path);
   bool ok = true;
   const uint32_t *ed = (const uint32_t *)g->edges;
   const size_t stride = g->esz / 4;
   if (bin) {
-    uint32_t hdr[2] = {g->n, g->m};
-    ok = fwrite(hdr, 4, 2, f) == 2 && fwrite(g->node_pointer, 4, g->n, f) == g->n;
+    const size_t npsz = bin64 ? 8 : 4;
+    if (bin64) {
+      const uint64_t hdr[2] = {g->n, g->m};
+      ok = fwrite(hdr, 8, 2, f) == 2;
+    } else {
+      const uint32_t hdr[2] = {g->n, (uint32_t)g->m};
+      ok = fwrite(hdr, 4, 2, f) == 2;
+    }
+    if (ok && (npsz == 8) == (g->node_pointer64 != nullptr)) {
+      const void *np = g->node_pointer64 ? (const void *)g->node_pointer64 : (const void *)g->node_pointer;
+      ok = fwrite(np, npsz, g->n, f) == g->n;
+    } else if (ok) {  // widen or narrow in blocks
+      std::vector<char> buf(npsz << 20);
+      for (uint32_t v0 = 0; ok && v0 < g->n; v0 += 1u << 20) {
+        const uint32_t k = std::min<uint32_t>(g->n - v0, 1u << 20);
+        for (uint32_t i = 0; i < k; ++i) {
+          const uint64_t x = np_at(g, uint64_t(v0) + i);
+          if (npsz == 8) reinterpret_cast<uint64_t *>(buf.data())[i] = x;
+          else reinterpret_cast<uint32_t *>(buf.data())[i] = (uint32_t)x;
+        }
+        ok = fwrite(buf.data(), npsz, k, f) == k;
+      }
+    }
     if (ok && want_w == (bool)g->weighted) {
       size_t total = size_t(g->m) * g->esz, done = 0;
       while (ok && done < total) {
@@ -715,26 +893,31 @@ int sgw_graph_save(const sgw_graph *g, const char *path) {
     // into their own buffers and written in order
     const int T = omp_get_max_threads();
     std::vector<std::string> bufs(T);
+    auto row_of = [&](uint32_t lo, uint32_t hi, uint64_t e) {  // last v in [lo, hi) with np[v] <= e
+      while (hi - lo > 1) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (np_at(g, mid) <= e) lo = mid; else hi = mid;
+      }
+      return lo;
+    };
     uint32_t v0 = 0;
     while (ok && v0 < g->n) {
-      const uint32_t e0 = g->node_pointer[v0];
-      uint32_t v1 = (uint32_t)(std::upper_bound(g->node_pointer + v0, g->node_pointer + g->n,
-                                                 uint64_t(e0) + (1u << 24)) - g->node_pointer);
-      v1 = std::max(v1, v0 + 1);
-      const uint64_t span = uint64_t(g->node_pointer[v1]) - e0;
+      const uint64_t e0 = np_at(g, v0);
+      uint32_t v1 = row_of(v0, g->n + 1, e0 + (1u << 24)) + 1;
+      v1 = std::min(std::max(v1, v0 + 1), g->n);
+      const uint64_t span = np_at(g, v1) - e0;
 #pragma omp parallel num_threads(T)
       {
         const int t = omp_get_thread_num(), nt = omp_get_num_threads();
-        const uint32_t lo_e = (uint32_t)(e0 + span * t / nt), hi_e = (uint32_t)(e0 + span * (t + 1) / nt);
+        const uint64_t lo_e = e0 + span * t / nt, hi_e = e0 + span * (t + 1) / nt;
         std::string &b = bufs[t];
         b.clear();
         b.reserve(size_t(hi_e - lo_e) * (want_w ? 24 : 20));
         // the vertex whose row holds edge lo_e
-        uint32_t v = (uint32_t)(std::upper_bound(g->node_pointer + v0, g->node_pointer + v1, lo_e) -
-                                g->node_pointer) - 1;
+        uint32_t v = row_of(v0, v1 + 1, lo_e);
         char tmp[40];
-        for (uint32_t i = lo_e; i < hi_e; ++i) {
-          while (g->node_pointer[v + 1] <= i) ++v;
+        for (uint64_t i = lo_e; i < hi_e; ++i) {
+          while (np_at(g, uint64_t(v) + 1) <= i) ++v;
           char *q = tmp;
           q = put_u32(q, v);
           *q++ = ' ';
@@ -757,9 +940,11 @@ void sgw_graph_free(sgw_graph *g) {
   if (!g) return;
   if (g->map_base) {
     host_free(g->node_pointer);
+    host_free(g->node_pointer64);
     munmap(g->map_base, g->map_len);
   } else if (g->owns) {
     host_free(g->node_pointer);
+    host_free(g->node_pointer64);
     host_free(g->edges);
   }
   delete g;
@@ -770,68 +955,49 @@ int sgw_graph_map(const char *path, sgw_graph **out) {
   if (!path || !out) return fail(SGW_EINVAL, "null argument");
   *out = nullptr;
   const std::string ext = extension_of(path);
-  if (ext != "bcsr" && ext != "bwcsr")
-    return fail(SGW_EFORMAT, "only .bcsr/.bwcsr files can be mapped: '%s'", path);
-  const int weighted = ext == "bwcsr";
+  const bool wide_file = ext == "bcsr64" || ext == "bwcsr64";
+  if (ext != "bcsr" && ext != "bwcsr" && !wide_file)
+    return fail(SGW_EFORMAT, "only .bcsr/.bwcsr(64) files can be mapped: '%s'", path);
+  const int weighted = ext == "bwcsr" || ext == "bwcsr64";
   int fd = open(path, O_RDONLY);
   if (fd < 0) return fail(SGW_EIO, "cannot open %s", path);
-  struct stat sb;
-  uint32_t hdr[2];
-  if (fstat(fd, &sb) != 0 || pread(fd, hdr, sizeof(hdr), 0) != (ssize_t)sizeof(hdr)) {
+  BinHeader h;
+  int st = read_header(fd, path, wide_file, weighted, &h);
+  if (st != SGW_OK) { close(fd); return st; }
+  const uint32_t n = (uint32_t)h.n, esz = weighted ? 8 : 4;
+  const size_t want = h.hdr + h.npsz * size_t(n) + size_t(h.m) * esz;
+  if (weighted && !wide_file && (n & 1u)) {  // 8-byte records would start 4 bytes off an 8-byte boundary
     close(fd);
-    return fail(SGW_EFORMAT, "%s: truncated header", path);
+    return load_binary(path, weighted, wide_file, out);
   }
-  const uint32_t n = hdr[0], m = hdr[1], esz = weighted ? 8 : 4;
-  const long long want = 8LL + 4LL * n + (long long)m * esz;
-  if (n == 0) { close(fd); return fail(SGW_EFORMAT, "%s: zero vertices", path); }
-  if ((long long)sb.st_size != want) {
-    close(fd);
-    return fail(SGW_EFORMAT, "%s: size %lld, expected %lld for n=%u m=%u", path,
-                (long long)sb.st_size, want, n, m);
-  }
-  if (weighted && (n & 1u)) {  // 8-byte records would start 4 bytes off an 8-byte boundary
-    close(fd);
-    return load_binary(path, weighted, out);
-  }
-  void *base = mmap(nullptr, (size_t)want, PROT_READ, MAP_SHARED, fd, 0);
+  void *base = mmap(nullptr, want, PROT_READ, MAP_SHARED, fd, 0);
   close(fd);
   if (base == MAP_FAILED) return fail(SGW_EIO, "cannot map %s", path);
-  madvise(base, (size_t)want, MADV_WILLNEED);
-  uint32_t *np = (uint32_t *)host_alloc(sizeof(uint32_t) * (size_t(n) + 1), nullptr);
+  madvise(base, want, MADV_WILLNEED);
+  // the node pointers are copied (u32 below 2^32 edges, else u64); the
+  // records stay in the mapping
+  const bool wide = h.m >= (uint64_t(1) << 32);
+  void *np = host_alloc((wide ? 8 : 4) * (size_t(n) + 1), nullptr);
   sgw_graph *g = np ? new (std::nothrow) sgw_graph() : nullptr;
   if (!g) {
     host_free(np);
-    munmap(base, (size_t)want);
+    munmap(base, want);
     return fail(SGW_ENOMEM, "graph arrays (n=%u)", n);
   }
-  const uint32_t *fnp = (const uint32_t *)((const char *)base + 8);
-#pragma omp parallel for
-  for (int64_t v = 0; v < (int64_t)n; ++v) np[v] = fnp[v];
-  np[n] = m;
   g->n = n;
-  g->m = m;
+  g->m = h.m;
   g->weighted = weighted;
   g->esz = esz;
   g->owns = false;
-  g->node_pointer = np;
-  g->edges = (char *)base + 8 + 4 * size_t(n);
+  if (wide) g->node_pointer64 = (uint64_t *)np;
+  else g->node_pointer = (uint32_t *)np;
+  const bool fits = fill_pointers(g, (const char *)base + h.hdr, h.npsz);
+  g->edges = (char *)base + h.hdr + h.npsz * size_t(n);
   g->map_base = base;
-  g->map_len = (size_t)want;
-  int bad = 0;
-#pragma omp parallel for reduction(| : bad)
-  for (int64_t v = 0; v < (int64_t)n; ++v)
-    if (np[v] > np[v + 1]) bad |= 1;
-  if (!bad) {
-    const uint32_t *ed = (const uint32_t *)g->edges;
-    const size_t stride = esz / 4;
-#pragma omp parallel for reduction(| : bad)
-    for (int64_t i = 0; i < (int64_t)m; ++i)
-      if (ed[size_t(i) * stride] >= n) bad |= 2;
-  }
-  if (bad) {
+  g->map_len = want;
+  if (const int bad = fits ? validate_csr(g) : 1) {
     sgw_graph_free(g);
-    return fail(SGW_EFORMAT, "%s: %s", path,
-                (bad & 1) ? "node pointers not monotone" : "edge endpoint out of range");
+    return fail(SGW_EFORMAT, "%s: %s", path, csr_problem(bad));
   }
   *out = g;
   return SGW_OK;
@@ -877,7 +1043,7 @@ int sgw_graph_symmetrize(const sgw_graph *g, sgw_graph **out) {
   std::vector<uint32_t> srcof(g->m);
 #pragma omp parallel for schedule(dynamic, 1024)
   for (int64_t v = 0; v < (int64_t)n; ++v)
-    for (uint32_t i = g->node_pointer[v]; i < g->node_pointer[v + 1]; ++i) srcof[i] = (uint32_t)v;
+    for (uint64_t i = np_at(g, (uint64_t)v), e = np_at(g, (uint64_t)v + 1); i < e; ++i) srcof[i] = (uint32_t)v;
   const uint64_t m = g->m;
   // vertex n-2 keeps no out-edges, as in the generators
   return build_csr(n, 2 * m,
@@ -907,7 +1073,7 @@ static void wcc_labels(const sgw_graph *g, std::vector<uint32_t> &root) {
   for (int64_t v = 0; v < (int64_t)n; ++v) par[v].store((uint32_t)v, std::memory_order_relaxed);
 #pragma omp parallel for schedule(dynamic, 4096)
   for (int64_t v = 0; v < (int64_t)n; ++v) {
-    for (uint32_t i = g->node_pointer[v]; i < g->node_pointer[v + 1]; ++i) {
+    for (uint64_t i = np_at(g, (uint64_t)v), e = np_at(g, (uint64_t)v + 1); i < e; ++i) {
       uint32_t a = (uint32_t)v, b = ed[size_t(i) * stride];
       while (true) {
         a = uf_find(par, a);
@@ -934,7 +1100,7 @@ int sgw_largest_wcc(const sgw_graph *g, uint32_t *vertices, uint64_t *edges) {
   std::vector<uint64_t> esum(g->n, 0);
   for (uint32_t v = 0; v < g->n; ++v) {
     size[root[v]]++;
-    esum[root[v]] += g->node_pointer[v + 1] - g->node_pointer[v];
+    esum[root[v]] += deg_at(g, v);
   }
   uint32_t best = 0;
   for (uint32_t v = 1; v < g->n; ++v)
@@ -956,7 +1122,7 @@ int sgw_pick_sources(const sgw_graph *g, uint32_t count, uint64_t seed, uint32_t
     if (size[v] > size[best]) best = v;
   std::vector<uint32_t> cand;
   for (uint32_t v = 0; v < g->n; ++v)
-    if (root[v] == best && g->node_pointer[v + 1] > g->node_pointer[v]) cand.push_back(v);
+    if (root[v] == best && deg_at(g, v) > 0) cand.push_back(v);
   if (cand.empty()) return fail(SGW_EINVAL, "no vertex with out-edges");
   SplitMix rng(mix64(seed ^ 0xa54ff53a5f1d36f1ULL));
   std::vector<uint32_t> chosen;

@@ -10,10 +10,15 @@
 
 struct sgw_graph {
   uint32_t n = 0;
-  uint32_t m = 0;
+  uint64_t m = 0;
   int weighted = 0;
   uint32_t esz = 4;               // bytes per edge record (4 or 8)
-  uint32_t *node_pointer = nullptr;  // n + 1 entries, node_pointer[n] == m
+  // n + 1 node pointers, [n] == m: u32 (node_pointer) for graphs of fewer
+  // than 2^32 edges, which every reader and generator produces; u64
+  // (node_pointer64) at 2^32 edges and above, and for a caller's u64 arrays
+  // (sgw_graph_from_csr64).  Exactly one of the two is set.
+  uint32_t *node_pointer = nullptr;
+  uint64_t *node_pointer64 = nullptr;
   void *edges = nullptr;          // m * esz bytes, page aligned when owned
   bool owns = false;              // arrays allocated (and freed) by the library
   size_t edges_bytes_alloc = 0;   // rounded allocation size of edges
@@ -27,6 +32,35 @@ struct sgw_graph {
 };
 
 namespace sgw {
+
+// Node pointer v of either width.
+inline uint64_t np_at(const sgw_graph *g, uint64_t v) {
+  return g->node_pointer64 ? g->node_pointer64[v] : (uint64_t)g->node_pointer[v];
+}
+// Out-degree of v (below 2^32: degrees are checked when a graph is made).
+inline uint32_t deg_at(const sgw_graph *g, uint64_t v) { return (uint32_t)(np_at(g, v + 1) - np_at(g, v)); }
+
+// Node pointers on the device: the low 32 bits of every one (degrees are
+// their differences) and, for graphs with u64 node pointers, the full pointer
+// of every 2^kOffGroupLog2-th vertex (obase, n / 2^kOffGroupLog2 + 2 entries).
+// No group of that many vertices spans 2^32 edges (checked when a graph is
+// given to an engine or a batch), so the low bits and the group's base give
+// the rest.
+constexpr uint32_t kOffGroupLog2 = 10;
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned long long off_at(const uint32_t *off, const unsigned long long *obase,
+                                                     uint32_t v) {
+  const uint32_t o = off[v];
+  if (!obase) return o;
+  const unsigned long long b = obase[v >> kOffGroupLog2];
+  return b + (uint32_t)(o - (uint32_t)b);
+}
+#endif
+// The device form of a graph's node pointers: lo[v] = low 32 bits of
+// np[v] (n + 1 entries) and, for u64 node pointers, base[k] = np[min(n, k <<
+// kOffGroupLog2)].  Returns false (filling nothing) when some group spans
+// 2^32 edges or more.
+bool device_offsets(const sgw_graph *g, uint32_t *lo, unsigned long long *base);
 
 // Records a status with a message for sgw_last_error() and returns it.
 int fail(int status, const char *fmt, ...);

@@ -25,6 +25,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "sgw_internal.h"
 #include "sgw_mlp.cuh"
 
@@ -220,6 +222,11 @@ struct GenArgs {
   uint32_t epoch;
   uint32_t num_tiles;
   int consume;               // sync: labels of queued vertices are cleared
+  // Count/write form: most edges one generate queues (0: no limit).  Only
+  // whole tiles are queued, in order, up to the limit (the first tile with
+  // edges always); the later tiles keep their labels, and the count pass
+  // leaves label clearing to the write pass of the tiles that are queued.
+  uint32_t edge_limit = 0;
   // PageRank form (activeness delta > acc instead of labels)
   double *delta;             // pending residual per vertex
   double *pval;              // accumulated rank per vertex
@@ -508,7 +515,7 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_count(GenArgs a) {
   GenLane L;
   if (v0 < a.n) {
     gen_lane(a, v0, full, L);
-    gen_clear(a, v0, full, L);
+    if (!a.edge_limit) gen_clear(a, v0, full, L);
     a.gmask[v0 / kGenVPerLane] = L.keepmask | (L.clearmask << 16);
   }
   const uint32_t seen = __reduce_add_sync(0xffffffffu, L.seen);
@@ -531,11 +538,81 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_count(GenArgs a) {
 // tincl, the totals into the control block and the pointer sentinel
 // (subgraph_generator.cu:160).
 constexpr int kGenScanThreads = 1024;
+
+// Exclusive prefix of x over the CTA's threads (kGenScanThreads), in thread order.
+__device__ __forceinline__ unsigned long long gen_block_excl(unsigned long long x, unsigned long long *s_warp) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  unsigned long long incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  __syncthreads();  // s_warp may still be read by a previous call
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const unsigned long long w = s_warp[lane];
+    unsigned long long wi = w;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= d) wi += y;
+    }
+    s_warp[lane] = wi - w;
+  }
+  __syncthreads();
+  return s_warp[warp] + incl - x;
+}
+
+// The scan under an edge limit: tile t is queued when the edges of the tiles
+// before it plus its own stay within the limit, or when no tile before it has
+// edges.  The queued tiles are a prefix (the edge prefix only grows); each
+// gets its (count, edges) prefix in tincl, the others ~0, and the last
+// queued tile writes the totals and the sentinel.
+__device__ __forceinline__ void gen_scan_limited(const GenArgs &a, uint32_t lo, uint32_t hi,
+                                                 unsigned long long *s_warp) {
+  unsigned long long sc = 0, se = 0;
+  for (uint32_t t = lo; t < hi; ++t) {
+    const unsigned long long x = a.tagg[t];
+    sc += x >> 32;
+    se += x & 0xffffffffull;
+  }
+  unsigned long long rc = gen_block_excl(sc, s_warp);
+  unsigned long long re = gen_block_excl(se, s_warp);
+  const unsigned long long lim = a.edge_limit;
+  for (uint32_t t = lo; t < hi; ++t) {
+    const unsigned long long x = a.tagg[t];
+    const unsigned long long ct = x >> 32, et = x & 0xffffffffull;
+    const bool in = re + et <= lim || re == 0;
+    a.tincl[t] = in ? ((rc << 32) | re) : ~0ull;
+    if (in) {
+      bool next_in = false;
+      if (t + 1 < a.num_tiles) {
+        const unsigned long long ne = re + et, en = a.tagg[t + 1] & 0xffffffffull;
+        next_in = ne + en <= lim || ne == 0;
+      }
+      if (!next_in) {
+        const uint32_t c = (uint32_t)(rc + ct);
+        a.ctl->num_active = c;
+        a.ctl->num_active_edges = re + et;
+        a.ptr[c] = (uint32_t)(re + et);
+      }
+    }
+    rc += ct;
+    re += et;
+  }
+}
+
 __global__ void __launch_bounds__(kGenScanThreads) k_generate_scan(GenArgs a) {
   __shared__ unsigned long long s_warp[kGenScanThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t per = (a.num_tiles + kGenScanThreads - 1) / kGenScanThreads;
   const uint32_t lo = min(a.num_tiles, tid * per), hi = min(a.num_tiles, lo + per);
+  if (a.edge_limit) {
+    gen_scan_limited(a, lo, hi, s_warp);
+    return;
+  }
   unsigned long long sum = 0;
   for (uint32_t t = lo; t < hi; ++t) sum += a.tagg[t];
   unsigned long long incl = sum;
@@ -579,9 +656,21 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_write(GenArgs a) {
   const uint32_t tile = blockIdx.x;
   const uint32_t v0 = tile * kGenTile + warp * (32 * kGenRounds) + lane * kGenVPerLane;
   const bool full = v0 + kGenVPerLane <= a.n;
+  if (a.edge_limit && a.tincl[tile] == ~0ull) return;  // beyond the limit: labels kept for later
   GenLane L;
   if (v0 < a.n) {
-    L.keepmask = a.gmask[v0 / kGenVPerLane] & 0xffffu;
+    const uint32_t gm = a.gmask[v0 / kGenVPerLane];
+    L.keepmask = gm & 0xffffu;
+    if (a.edge_limit && (gm >> 16)) {  // the clearing the count pass left to this tile
+      L.clearmask = gm >> 16;
+      if (full) {
+        const uint4 x = *reinterpret_cast<const uint4 *>(a.l1 + v0);
+        const uint4 y = *reinterpret_cast<const uint4 *>(a.l2 + v0);
+        L.l1w[0] = x.x; L.l1w[1] = x.y; L.l1w[2] = x.z; L.l1w[3] = x.w;
+        L.l2w[0] = y.x; L.l2w[1] = y.y; L.l2w[2] = y.z; L.l2w[3] = y.w;
+      }
+      gen_clear(a, v0, full, L);
+    }
     if (L.keepmask) {
       if (full) {
 #pragma unroll
@@ -840,14 +929,15 @@ __device__ __forceinline__ uint32_t warp_last_le(const uint32_t *__restrict__ pt
 // in shared memory and every thread copies edges by binary search in it.
 // Consecutive threads read consecutive host edges of one source, so host
 // reads are coalesced; E is the edge record (one or two u32 words).
-template <int W>
+template <int W, bool WIDE>
 __global__ void __launch_bounds__(kGatherThreads) k_gather(
     const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
-    const uint32_t *__restrict__ off, HostChunks host_edges,
+    const uint32_t *__restrict__ off, const unsigned long long *__restrict__ obase, HostChunks host_edges,
     uint32_t *__restrict__ buf, uint32_t from, uint32_t size, uint32_t edge_from,
     uint32_t edge_count) {
+  using HP = typename std::conditional<WIDE, unsigned long long, uint32_t>::type;
   __shared__ uint32_t s_bpos[kScalarGatherTile + 1];
-  __shared__ uint32_t s_hpos[kScalarGatherTile + 1];
+  __shared__ HP s_hpos[kScalarGatherTile + 1];
   __shared__ uint32_t s_first, s_last;
   const uint32_t ntiles = (edge_count + kScalarGatherTile - 1) / kScalarGatherTile;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -864,7 +954,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(
     for (uint32_t k = threadIdx.x; k < nsrc; k += blockDim.x) {
       const uint32_t i = first + k;
       s_bpos[k] = ptr[i] - edge_from;
-      s_hpos[k] = off[queue[i]];
+      s_hpos[k] = WIDE ? (HP)off_at(off, obase, queue[i]) : (HP)off[queue[i]];
     }
     __syncthreads();
     // four independent host loads in flight per thread before any store
@@ -913,9 +1003,8 @@ template <uint32_t R>
 __device__ __forceinline__ uint32_t gather_scan(uint32_t nsrc, const uint32_t *s_hlo, const uint32_t *s_len,
                                                 uint32_t *s_cs, uint32_t *s_part) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  auto chunks = [&](uint32_t k) {
-    const uint32_t hlo = s_hlo[k], len = s_len[k];
-    return (hlo + len + R - 1) / R - hlo / R;
+  auto chunks = [&](uint32_t k) {  // depends on the source's record mod R only
+    return (s_hlo[k] % R + s_len[k] + R - 1) / R;
   };
   uint32_t part = 0;
   for (uint32_t q = 0; q < kGatherPer; ++q) {
@@ -941,24 +1030,30 @@ __device__ __forceinline__ uint32_t gather_scan(uint32_t nsrc, const uint32_t *s
 }
 
 // Copies the tile's chunks of RB-byte records: RB 4 / 8 straight into buf,
-// RB 1 into the shared byte tile at position - j0.
-template <int RB>
+// RB 1 into the shared byte tile at position - j0.  A source's first record
+// is (s_hhi:s_hlo), s_hhi only with WIDE; a chunk's records are matched to
+// the source by their distance from it, which fits 32 bits.
+template <int RB, bool WIDE>
 __device__ __forceinline__ void gather_copy(uint32_t total, uint32_t nsrc, uint32_t j0, const uint32_t *s_cs,
-                                            const uint32_t *s_hlo, const uint32_t *s_len, const uint32_t *s_bpos,
-                                            const HostChunks &host16, void *__restrict__ buf,
-                                            uint8_t *s_bytes) {
+                                            const uint32_t *s_hlo, const uint32_t *s_hhi, const uint32_t *s_len,
+                                            const uint32_t *s_bpos, const HostChunks &host16,
+                                            void *__restrict__ buf, uint8_t *s_bytes) {
+  using CT = typename std::conditional<WIDE, unsigned long long, uint32_t>::type;
   constexpr uint32_t R = 16 / RB;
   constexpr int U = 4;
   for (uint32_t jb = threadIdx.x; jb < total; jb += U * blockDim.x) {
     uint4 v[U];
-    uint32_t kk[U], cc[U];
+    uint32_t kk[U];
+    CT cc[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const uint32_t j = jb + u * blockDim.x;
       kk[u] = 0xffffffffu;
       if (j < total) {
         const uint32_t k = last_le(s_cs, nsrc, j);
-        const uint32_t c = s_hlo[k] / R + (j - s_cs[k]);
+        CT h = s_hlo[k];
+        if (WIDE) h |= (CT)s_hhi[k] << (WIDE ? 32 : 0);
+        const CT c = h / R + (j - s_cs[k]);
         kk[u] = k;
         cc[u] = c;
         v[u] = *reinterpret_cast<const uint4 *>(hc_at(host16, (size_t)c << 4));
@@ -968,13 +1063,15 @@ __device__ __forceinline__ void gather_copy(uint32_t total, uint32_t nsrc, uint3
     for (int u = 0; u < U; ++u) {
       if (kk[u] == 0xffffffffu) continue;
       const uint32_t k = kk[u];
-      const uint32_t hlo = s_hlo[k], len = s_len[k], bpos = s_bpos[k];
+      const uint32_t len = s_len[k], bpos = s_bpos[k];
+      // distance of the chunk's first record from the source's first (mod 2^32)
+      const uint32_t d0 = (uint32_t)cc[u] * R - s_hlo[k];
       const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
 #pragma unroll
       for (uint32_t r = 0; r < R; ++r) {
-        const uint32_t rec = cc[u] * R + r;
-        if (rec >= hlo && rec - hlo < len) {
-          const uint32_t o = bpos + (rec - hlo);
+        const uint32_t d = d0 + r;
+        if (d < len) {
+          const uint32_t o = bpos + d;
           if (RB == 4) reinterpret_cast<uint32_t *>(buf)[o] = w[r];
           else if (RB == 8) reinterpret_cast<uint2 *>(buf)[o] = make_uint2(w[2 * r], w[2 * r + 1]);
           else s_bytes[o - j0] = (uint8_t)(w[r / 4] >> (8 * (r % 4)));
@@ -985,14 +1082,16 @@ __device__ __forceinline__ void gather_copy(uint32_t total, uint32_t nsrc, uint3
 }
 
 // Dynamic shared memory of k_gather_v: four u32 arrays of kGatherTile + 1
-// entries, the scan partials, then (16-byte aligned) the tile's weight bytes.
+// entries, the scan partials, then (16-byte aligned) the tile's weight bytes;
+// the WIDE form adds the high words of the sources' host positions.
 constexpr size_t kGatherBytesOff = ((4 * (kGatherTile + 1) + kGatherThreads + 1) * 4 + 15) / 16 * 16;
 constexpr size_t kGatherSmemBytes = kGatherBytesOff + kGatherTile;
+constexpr size_t kGatherSmemBytesWide = kGatherSmemBytes + ((kGatherTile + 1) * 4 + 15) / 16 * 16;
 
-template <int RB, bool WS>
+template <int RB, bool WS, bool WIDE>
 __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
     const uint32_t *__restrict__ queue, const uint32_t *__restrict__ ptr,
-    const uint32_t *__restrict__ off, HostChunks host16,
+    const uint32_t *__restrict__ off, const unsigned long long *__restrict__ obase, HostChunks host16,
     void *__restrict__ buf, HostChunks host_w16, uint8_t *__restrict__ wbuf,
     uint32_t from, uint32_t size, uint32_t edge_from, uint32_t edge_count) {
   extern __shared__ __align__(16) unsigned char g_gather_smem[];
@@ -1002,6 +1101,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
   uint32_t *const s_cs = s_len + (kGatherTile + 1);
   uint32_t *const s_part = s_cs + (kGatherTile + 1);
   uint8_t *const s_bytes = g_gather_smem + kGatherBytesOff;
+  uint32_t *const s_hhi = WIDE ? reinterpret_cast<uint32_t *>(g_gather_smem + kGatherSmemBytes) : nullptr;
   __shared__ uint32_t s_first, s_last;
   const uint32_t ntiles = (edge_count + kGatherTile - 1) / kGatherTile;
   const int tid = threadIdx.x;
@@ -1025,17 +1125,23 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_v(
         const uint32_t bp = ptr[i] - edge_from, be = ptr[i + 1] - edge_from;
         const uint32_t lo = max(bp, j0), hi = min(be, j1);
         s_bpos[k] = lo;
-        s_hlo[k] = off[queue[i]] + (lo - bp);
+        if (WIDE) {
+          const unsigned long long h = off_at(off, obase, queue[i]) + (lo - bp);
+          s_hlo[k] = (uint32_t)h;
+          s_hhi[k] = (uint32_t)(h >> 32);
+        } else {
+          s_hlo[k] = off[queue[i]] + (lo - bp);
+        }
         s_len[k] = hi - lo;
       }
     }
     __syncthreads();
     uint32_t total = gather_scan<16 / RB>(nsrc, s_hlo, s_len, s_cs, s_part);
-    gather_copy<RB>(total, nsrc, j0, s_cs, s_hlo, s_len, s_bpos, host16, buf, s_bytes);
+    gather_copy<RB, WIDE>(total, nsrc, j0, s_cs, s_hlo, s_hhi, s_len, s_bpos, host16, buf, s_bytes);
     if (WS) {
       __syncthreads();  // s_cs is reused
       total = gather_scan<16>(nsrc, s_hlo, s_len, s_cs, s_part);
-      gather_copy<1>(total, nsrc, j0, s_cs, s_hlo, s_len, s_bpos, host_w16, nullptr, s_bytes);
+      gather_copy<1, WIDE>(total, nsrc, j0, s_cs, s_hlo, s_hhi, s_len, s_bpos, host_w16, nullptr, s_bytes);
       __syncthreads();
       uint8_t *dst = wbuf + j0;
       const uint32_t len = j1 - j0;
@@ -1791,7 +1897,8 @@ __global__ void k_pr_init(uint32_t n, double init, double *pval, double *delta) 
 
 // ---- learned scheduler: per-range statistics and prediction -------------------
 struct RangeInfo {           // a static vertex range [v0, v1) with edges [e0, e1)
-  uint32_t v0, v1, e0, e1;
+  uint32_t v0, v1;
+  unsigned long long e0, e1;
 };
 
 struct RangeStat {           // one global iteration of one range

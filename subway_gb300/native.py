@@ -38,7 +38,7 @@ class EngineOpts(C.Structure):
                 ("chunk_edges", C.c_uint32), ("gather_ctas", C.c_uint32), ("num_buffers", C.c_uint32),
                 ("sched_inner", C.c_uint32), ("sched_active_permille", C.c_uint32),
                 ("sched_flags", C.c_uint32), ("sched_defer_permille", C.c_uint32),
-                ("transfer_chunk_log2", C.c_uint32), ("reserved", C.c_uint32)]
+                ("transfer_chunk_log2", C.c_uint32), ("generate_edge_limit", C.c_uint32)]
 
 
 class RunParams(C.Structure):
@@ -73,8 +73,11 @@ _PROTOS = {
     "sgw_graph_load": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "sgw_graph_map": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "sgw_graph_from_csr": (C.c_int, [C.c_uint32, C.c_uint32, _P, _P, C.c_int, C.POINTER(_P)]),
+    "sgw_graph_from_csr64": (C.c_int, [C.c_uint32, C.c_uint64, _P, _P, C.c_int, C.POINTER(_P)]),
     "sgw_graph_info": (C.c_int, [_P, _u32p, _u32p, C.POINTER(C.c_int)]),
+    "sgw_graph_info64": (C.c_int, [_P, _u32p, C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
     "sgw_graph_node_pointer": (_P, [_P]),
+    "sgw_graph_node_pointer64": (_P, [_P]),
     "sgw_graph_edges": (_P, [_P]),
     "sgw_graph_out_degree": (C.c_int, [_P, _P]),
     "sgw_graph_save": (C.c_int, [_P, C.c_char_p]),
@@ -195,8 +198,8 @@ class Graph:
     def __init__(self, handle: int, keep=None):
         self.h = C.c_void_p(handle)
         self._keep = keep
-        n, m, w = C.c_uint32(), C.c_uint32(), C.c_int()
-        check(lib().sgw_graph_info(self.h, C.byref(n), C.byref(m), C.byref(w)), "sgw_graph_info")
+        n, m, w = C.c_uint32(), C.c_uint64(), C.c_int()
+        check(lib().sgw_graph_info64(self.h, C.byref(n), C.byref(m), C.byref(w)), "sgw_graph_info64")
         self.n, self.m, self.weighted = n.value, m.value, bool(w.value)
 
     # ---- constructors
@@ -221,14 +224,17 @@ class Graph:
 
     @classmethod
     def map(cls, path):
-        """A .bcsr/.bwcsr file mapped in place: edges stay in the page cache."""
+        """A .bcsr/.bwcsr(64) file mapped in place: edges stay in the page cache."""
         h = _P()
         check(lib().sgw_graph_map(str(path).encode(), C.byref(h)), f"sgw_graph_map({path})")
         return cls(h.value)
 
     @classmethod
     def from_csr(cls, node_pointer, edges, weighted):
-        npa = np.ascontiguousarray(node_pointer, dtype=np.uint32)
+        """Wraps numpy CSR arrays without copying; u64 node pointers (or more
+        than 2^32 - 1 edges) give a graph with u64 node pointers."""
+        wide = np.asarray(node_pointer).dtype == np.uint64 or int(np.asarray(node_pointer)[-1]) >= 2 ** 32
+        npa = np.ascontiguousarray(node_pointer, dtype=np.uint64 if wide else np.uint32)
         eda = np.ascontiguousarray(edges, dtype=np.uint32)
         n = len(npa) - 1
         m = int(npa[-1])
@@ -237,15 +243,20 @@ class Graph:
         if eda.shape[0] != m:
             raise ValueError("edge count does not match node_pointer[-1]")
         h = _P()
-        check(lib().sgw_graph_from_csr(n, m, _ptr(npa), _ptr(eda) if m else None, int(weighted), C.byref(h)),
-              "sgw_graph_from_csr")
+        fn = lib().sgw_graph_from_csr64 if wide else lib().sgw_graph_from_csr
+        check(fn(n, m, _ptr(npa), _ptr(eda) if m else None, int(weighted), C.byref(h)),
+              "sgw_graph_from_csr64" if wide else "sgw_graph_from_csr")
         return cls(h.value, keep=(npa, eda))
 
     # ---- views
     @property
     def node_pointer(self) -> np.ndarray:
+        """(n + 1,) node pointers: u32, or u64 for a graph that holds u64 ones."""
         p = lib().sgw_graph_node_pointer(self.h)
-        return np.ctypeslib.as_array(C.cast(p, _u32p), shape=(self.n + 1,))
+        if p:
+            return np.ctypeslib.as_array(C.cast(p, _u32p), shape=(self.n + 1,))
+        p = lib().sgw_graph_node_pointer64(self.h)
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint64)), shape=(self.n + 1,))
 
     @property
     def edges(self) -> np.ndarray:
