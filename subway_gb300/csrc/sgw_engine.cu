@@ -376,12 +376,12 @@ struct Layout {
 };
 
 Layout make_layout(int fam, uint32_t n, uint64_t m, uint32_t esz, uint32_t nbuf,
-                   uint32_t num_tiles, uint64_t cap, uint32_t chunk, uint32_t tdm) {
+                   uint32_t num_tiles, uint64_t cap, uint32_t chunk, uint32_t tdm, bool wide) {
   Layout L{};
   size_t p = 0;
   auto take = [&](size_t bytes) { size_t at = p; p += align_up(bytes, 256); return at; };
   L.off = take(4ull * (n + 1));
-  L.obase = take(8ull * ((n >> kOffGroupLog2) + 2));
+  L.obase = take(wide ? 8ull * ((n >> kOffGroupLog2) + 2) : 0);
   L.tflag = take(4ull * num_tiles);
   L.tagg = take(8ull * num_tiles);
   L.tincl = take(8ull * num_tiles);
@@ -416,9 +416,9 @@ Layout make_layout(int fam, uint32_t n, uint64_t m, uint32_t esz, uint32_t nbuf,
 
 // Largest edge-buffer capacity whose layout fits `bytes` (0 if none does).
 uint64_t fit_cap(int fam, const sgw_engine_opts &o, uint32_t n, uint64_t m, uint32_t esz,
-                 uint32_t nbuf, uint32_t num_tiles, uint64_t bytes) {
+                 uint32_t nbuf, uint32_t num_tiles, uint64_t bytes, bool wide) {
   auto total = [&](uint64_t cap) {
-    return (uint64_t)make_layout(fam, n, m, esz, nbuf, num_tiles, cap, o.chunk_edges, o.tile_degree_max).total;
+    return (uint64_t)make_layout(fam, n, m, esz, nbuf, num_tiles, cap, o.chunk_edges, o.tile_degree_max, wide).total;
   };
   // max_partition_size <= DIST_INFINITY, and no larger than the whole graph
   const uint64_t hi_cap = std::min<uint64_t>(std::max<uint64_t>(m, 64), 4294967294ull);
@@ -441,7 +441,7 @@ uint64_t fit_cap(int fam, const sgw_engine_opts &o, uint32_t n, uint64_t m, uint
 
 int carve(sgw_engine *e, int fam, uint64_t cap) {
   const Layout L = make_layout(fam, e->n, e->m, e->rec_bytes, e->nbuf, e->num_tiles, cap,
-                               e->opts.chunk_edges, e->opts.tile_degree_max);
+                               e->opts.chunk_edges, e->opts.tile_degree_max, e->wide);
   if (L.total > e->arena_bytes) return fail(SGW_EBUDGET, "layout exceeds the arena");
   char *b = e->d_arena;
   e->d_off = (uint32_t *)(b + L.off);
@@ -1423,27 +1423,27 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   size_t need = 0;
   for (int fam = 0; fam < 2; ++fam)
     need = std::max(need, make_layout(fam, e->n, e->m, esz, e->nbuf, e->num_tiles, mfull,
-                                      o.chunk_edges, o.tile_degree_max).total);
+                                      o.chunk_edges, o.tile_degree_max, e->wide).total);
   uint64_t budget = o.budget_bytes;
   if (budget == 0) {
     // Subway's rule: 0.9 * (totalGlobalMem - 32 n) bytes of edges
     // (shared/subgraph.cu:24), here on top of the engine's own vertex state.
     const Layout L0 = make_layout(FAM_PR, e->n, e->m, esz, e->nbuf, e->num_tiles, mfull,
-                                  o.chunk_edges, o.tile_degree_max);
+                                  o.chunk_edges, o.tile_degree_max, e->wide);
     const double state = (double)L0.total - (double)e->nbuf * mfull * esz;  // all but the buffers
     double edges_bytes = 0.9 * ((double)prop.totalGlobalMem - 32.0 * e->n);
     budget = (uint64_t)(state + std::max(0.0, edges_bytes));
   }
   const size_t arena = (size_t)std::min<uint64_t>(budget, need);
   for (int fam = 0; fam < 2; ++fam) {
-    e->cap_fam[fam] = fit_cap(fam, o, e->n, e->m, esz, e->nbuf, e->num_tiles, arena);
+    e->cap_fam[fam] = fit_cap(fam, o, e->n, e->m, esz, e->nbuf, e->num_tiles, arena, e->wide);
     // split form: the weight bytes start at 4 * cap past a 256-byte aligned
     // buffer; a multiple of 4 keeps them 16-byte aligned for vector stores
     if (e->split && e->cap_fam[fam] > 16) e->cap_fam[fam] &= ~3ull;
   }
   if (e->cap_fam[FAM_INT] == 0) {
     const Layout L0 = make_layout(FAM_INT, e->n, e->m, esz, e->nbuf, e->num_tiles, 4096,
-                                  o.chunk_edges, o.tile_degree_max);
+                                  o.chunk_edges, o.tile_degree_max, e->wide);
     delete e;
     return fail(SGW_EBUDGET, "budget %llu B < vertex state and minimum edge buffers (about %zu B)",
                 (unsigned long long)budget, L0.total);
@@ -1460,7 +1460,7 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   for (int fam = 0; fam < 2; ++fam)
     if (e->cap_fam[fam])
       parts_host = std::max(parts_host, make_layout(fam, e->n, e->m, esz, e->nbuf, e->num_tiles,
-                                                    e->cap_fam[fam], o.chunk_edges, o.tile_degree_max).max_parts);
+                                                    e->cap_fam[fam], o.chunk_edges, o.tile_degree_max, e->wide).max_parts);
 
   int st = SGW_OK;
   auto cleanup = [&](int s) { sgw_engine_destroy(e); return s; };

@@ -181,7 +181,7 @@ def test_hub_larger_than_budget(gpu, orc):
     w = (1 + (src * 7 + dst * 13) % 50).astype(np.uint32)
     edges = np.stack([dst.astype(np.uint32), w], 1)
     g = gpu.Graph.from_csr(npt, edges, True)
-    eng = gpu.Engine(g, budget_bytes=18 * n + 13 * 1024 + 1000 * 16)
+    eng = gpu.Engine(g, budget_bytes=18 * n + 15 * 1024 + 1000 * 16)
     assert eng.max_partition_size() < 2500
     for algo in ("bfs", "sssp", "sswp", "cc"):
         for mode in MODES:

@@ -65,7 +65,7 @@ def test_u64_hub_and_batch(gpu, orc):
     npt = np.cumsum(npt).astype(np.uint64)
     w = (1 + (pairs[:, 0] * 7 + pairs[:, 1] * 13) % 50).astype(np.uint32)
     g = gpu.Graph.from_csr(npt, np.stack([pairs[:, 1].astype(np.uint32), w], 1), True)
-    eng = gpu.Engine(g, budget_bytes=18 * n + 13 * 1024 + 1000 * 16)
+    eng = gpu.Engine(g, budget_bytes=18 * n + 15 * 1024 + 1000 * 16)
     assert eng.max_partition_size() < 2500
     for algo in ALGS:
         for mode in MODES:
