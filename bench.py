@@ -22,7 +22,10 @@ which isolates what the network adds to the schedule's rules.
             engine creation (device arena, transfer copy of the host edges),
             sgw_run through the C ABI with host buffers (state init, every
             host->device edge transfer, the distance read-back) and engine
-            destruction; the graph load is excluded on both arms
+            destruction; the graph load is excluded on both arms.  The engine
+            is made as the drop-in apps make it, with its transfer copy in
+            pageable pages (SGW_OPT_PAGEABLE_COPY: half the set-up time);
+            e2e_pinned is the same with the pinned copy, the library default
   e2e_warm  sgw_run alone on a live engine (a resident query service)
 After the timed loops every distinct source's distances from every schedule
 are compared with the OpenMP oracle; the line carries the mismatch count and
@@ -261,9 +264,9 @@ def run_ours(a, dist):
     out = np.empty(g.n, np.uint32)  # host result buffer
     nb_learned = a.num_buffers or N.sched_buffers(g, a.budget)
 
-    def make_engine(arm):
+    def make_engine(arm, extra_flags=0):
         nb = 0 if arm == "plain" else nb_learned
-        e = N.Engine(g, budget_bytes=int(a.budget), device=dev, flags=flags, gather_ctas=a.gather_ctas,
+        e = N.Engine(g, budget_bytes=int(a.budget), device=dev, flags=flags | extra_flags, gather_ctas=a.gather_ctas,
                      tile_degree_max=a.tile_degree_max, chunk_edges=a.chunk_edges,
                      inner_batch=a.inner_batch, num_buffers=nb, sched_inner=a.sched_inner,
                      sched_active_permille=a.sched_permille, sched_defer_permille=a.sched_defer)
@@ -354,20 +357,24 @@ def run_ours(a, dist):
         eng.close()
         del eng
 
-    # one query as a process runs it: create, run with host buffers, destroy
-    for arm in [x for x in ("plain", "learned") if x in arms]:
+    # one query as a process runs it: create, run with host buffers, destroy;
+    # the engine made as the drop-in apps make it (transfer copy in pageable
+    # pages), and for the learned schedule also with the pinned copy
+    e2e_loops = [(arm, "e2e", N.OPT_PAGEABLE_COPY) for arm in ("plain", "learned") if arm in arms]
+    e2e_loops += [("learned", "e2e_pinned", 0)] if "learned" in arms else []
+    for arm, key, xf in e2e_loops:
         walls, st_all = [], []
         for k in range(a.warmup + a.steps):
             t = time.perf_counter()
-            eng = make_engine(arm)
+            eng = make_engine(arm, xf)
             _, st = eng.run(a.algo, a.mode, sources[k % len(sources)], out=out)
             eng.close()
             w = time.perf_counter() - t
             if k >= a.warmup:
                 walls.append(w)
                 st_all.append(st)
-        res[arm]["e2e_walls"] = walls
-        res[arm]["e2e_reached"] = sum(s["reached_edges"] for s in st_all)
+        res[arm][key + "_walls"] = walls
+        res[arm][key + "_reached"] = sum(s["reached_edges"] for s in st_all)
     refs.clear()
 
     hbm_peak, hbm_src = measured_peaks()
@@ -385,9 +392,10 @@ def run_ours(a, dist):
              "ms_per_step": round(dev_ms / K, 4),
              "iterations_per_step": round(sum(s["global_iterations"] for s in steps) / K, 2),
              "engine_create_s": round(r["create_s"], 3)}
-        if "e2e_walls" in r:
-            d["e2e"] = round(dist.sum(r["e2e_reached"]) / (dist.max(sum(r["e2e_walls"])) * 1e9), 4)
-            d["e2e_ms_per_step"] = round(1e3 * sum(r["e2e_walls"]) / len(r["e2e_walls"]), 2)
+        for key in ("e2e", "e2e_pinned"):
+            if key + "_walls" in r:
+                d[key] = round(dist.sum(r[key + "_reached"]) / (dist.max(sum(r[key + "_walls"])) * 1e9), 4)
+                d[key + "_ms_per_step"] = round(1e3 * sum(r[key + "_walls"]) / len(r[key + "_walls"]), 2)
         return d
 
     head = "learned" if "learned" in arms else "plain"
@@ -444,7 +452,10 @@ def run_ours(a, dist):
                      "transfer_record_bytes": esz},
         "e2e": {"value": hs.get("e2e"), "unit": "GTEPS", "h2d_bytes_per_step": int(h2d_e2e),
                 "d2h_bytes_per_step": d2h_e2e, "ms_per_step": hs.get("e2e_ms_per_step"),
-                "includes": "engine creation (arena, transfer copy), sgw_run with host buffers, engine destruction"},
+                "includes": "engine creation (arena, transfer copy), sgw_run with host buffers, engine destruction",
+                "transfer_copy": "pageable pages, as the drop-in apps make it (SGW_OPT_PAGEABLE_COPY)"},
+        "e2e_pinned": {"value": hs.get("e2e_pinned"), "unit": "GTEPS", "ms_per_step": hs.get("e2e_pinned_ms_per_step"),
+                       "transfer_copy": "pinned (cudaHostAlloc), the library default"},
         "e2e_warm": {"value": hs["e2e_warm"], "unit": "GTEPS", "ms_per_step":
                      round(dist.max(sum(s["wall_ms"] for s in steps)) / K, 4)},
         "mismatches": check["mismatches"] if a.check == "all" else None,

@@ -144,6 +144,16 @@ void sgw_graph_free(sgw_graph *g);
  * the graph (measured best); these flags force one form for both. */
 #define SGW_OPT_BATCH_PERSISTENT 0x40u
 #define SGW_OPT_BATCH_GRAPH 0x80u
+/* The engine's host transfer copy in ordinary pageable pages instead of
+ * pinned cudaHostAlloc memory, on devices that read pageable memory through
+ * the host page tables (GB300 with its Grace host; elsewhere the flag is
+ * ignored): the filling threads' first touch replaces the driver's page
+ * pinning, so engine creation and destruction take about half as long (RMAT-28:
+ * 0.47-0.58 s against 1.0-1.08 s to create, 0.08 against 0.16 s to destroy),
+ * while a run is as fast under the plain schedule and 4-7% slower under the
+ * learned one.  Whole-range and hub copies then run as a copy kernel instead
+ * of DMA.  The drop-in apps, which answer one query per process, set it. */
+#define SGW_OPT_PAGEABLE_COPY 0x100u
 /* sched_flags: the learned policy's inner cap also covers compacted ranges */
 #define SGW_SCHED_CAP_COMPACT 0x1u
 /* sched_flags: transfer active vertices that cannot push, as the reference's

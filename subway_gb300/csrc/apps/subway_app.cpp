@@ -206,6 +206,7 @@ int main(int argc, char **argv) {
   sgw_engine_opts_default(&o);
   o.budget_bytes = a.budget;
   o.device = a.device;
+  o.flags |= SGW_OPT_PAGEABLE_COPY;  // one query per process: the cheaper transfer copy to set up
   if (!a.scheduler.empty() && a.budget) sgw_sched_buffers(g, a.budget, &o.num_buffers);
   sgw_engine *e = nullptr;
   st = sgw_engine_create(g, &o, &e);

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
+#include <sys/mman.h>
 
 #include <algorithm>
 #include <atomic>
@@ -55,6 +56,8 @@ struct HostStream {
   std::vector<unsigned long long> d;   // device addresses of the chunks
   uint32_t shift = 30;
   size_t bytes = 0;                    // data bytes
+  bool pageable = false;               // chunks are ordinary pages, read through the host page tables
+  const unsigned long long *dtab = nullptr;  // the chunk table on the device
 };
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -209,9 +212,19 @@ int check_ctl_error(sgw_engine *e) {
   return fail(SGW_ECUDA, "device error code %u", err);
 }
 
-// DMA copy of bytes [off, off + bytes) of a host stream, one cudaMemcpyAsync
-// per chunk it touches.
+// Copy of bytes [off, off + bytes) of a host stream: one DMA cudaMemcpyAsync
+// per chunk it touches, or for pageable chunks one k_copy_host launch (a DMA
+// copy from pageable memory is staged through the calling thread, which would
+// stall the pipeline).
 int copy_from_host(const HostStream &hs, void *dst, size_t off, size_t bytes, cudaStream_t st) {
+  if (hs.pageable) {
+    if (!bytes) return SGW_OK;
+    const unsigned long long words = ((off + bytes + 15) >> 4) - (off >> 4);
+    const uint32_t grid = (uint32_t)std::min<unsigned long long>((words + 255) / 256, 1216);
+    k_copy_host<<<grid, 256, 0, st>>>(HostChunks{hs.dtab, hs.shift}, off, bytes, static_cast<uint8_t *>(dst));
+    CK(cudaGetLastError());
+    return SGW_OK;
+  }
   char *d = static_cast<char *>(dst);
   const size_t cb = size_t(1) << hs.shift;
   while (bytes) {
@@ -269,7 +282,14 @@ cudaError_t alloc_and_fill(HostStream &a, HostStream &b, Fill fill) {
       HostStream &hs = *items[i].first;
       const size_t k = items[i].second;
       void *p = nullptr;
-      const cudaError_t ce = cudaHostAlloc(&p, hs.size[k], cudaHostAllocMapped | cudaHostAllocPortable);
+      cudaError_t ce = cudaSuccess;
+      if (hs.pageable) {  // ordinary pages, first touched (zeroed) by the filling threads
+        p = mmap(nullptr, hs.size[k], PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+        if (p == MAP_FAILED) { p = nullptr; ce = cudaErrorMemoryAllocation; }
+        else madvise(p, hs.size[k], MADV_NOHUGEPAGE);
+      } else {
+        ce = cudaHostAlloc(&p, hs.size[k], cudaHostAllocMapped | cudaHostAllocPortable);
+      }
       if (ce != cudaSuccess) {
         err[t] = ce;
         stop.store(1);
@@ -296,11 +316,15 @@ cudaError_t alloc_and_fill(HostStream &a, HostStream &b, Fill fill) {
 
 // Frees both streams' chunks, two at a time (as they were allocated).
 void free_streams(HostStream &a, HostStream &b) {
-  std::vector<char *> all;
-  for (char *p : a.h) if (p) all.push_back(p);
-  for (char *p : b.h) if (p) all.push_back(p);
+  std::vector<std::pair<char *, size_t>> all;  // (chunk, bytes if pageable else 0)
+  for (HostStream *hs : {&a, &b})
+    for (size_t k = 0; k < hs->h.size(); ++k)
+      if (hs->h[k]) all.push_back({hs->h[k], hs->pageable ? hs->size[k] : 0});
   auto work = [&](size_t t) {
-    for (size_t i = t; i < all.size(); i += 2) cudaFreeHost(all[i]);
+    for (size_t i = t; i < all.size(); i += 2) {
+      if (all[i].second) munmap(all[i].first, all[i].second);
+      else cudaFreeHost(all[i].first);
+    }
   };
   if (all.size() > 1) {
     std::thread other(work, 1);
@@ -337,7 +361,7 @@ int probe_stream_dma(sgw_engine *e) {
   int st = SGW_OK;
   for (int i = 0; i < 4 && st == SGW_OK; ++i) {  // the first copy warms up
     cudaEventRecord(a, e->s_copy);
-    cudaMemcpyAsync(e->d_buf[0], e->hs_ends.h[0], bytes, cudaMemcpyHostToDevice, e->s_copy);
+    st = copy_from_host(e->hs_ends, e->d_buf[0], 0, bytes, e->s_copy);
     cudaEventRecord(b, e->s_copy);
     if (cudaEventSynchronize(b) != cudaSuccess) { st = fail(SGW_ECUDA, "transfer-copy DMA probe"); break; }
     float ms = 0;
@@ -1467,17 +1491,26 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   // The transfer copy: the edge records (packed when they fit) in pinned,
   // mapped host memory from cudaHostAlloc, read in place by the gather
   // kernels and by DMA copies, in chunks (HostStream) so that two host
-  // threads can allocate it at once.  Ordinary pages written by all host
-  // threads and then registered with cudaHostRegister cost less to set up
-  // (0.5 s against 1.2 s for the 21 GB copy of RMAT-28 on a GB300 host), but
-  // the GPU then reached them through host page-table translations: the
-  // plain schedule's gathers, which touch rows all over the copy, ran at 7-9
-  // GB/s instead of 130-170 GB/s.
+  // threads can allocate it at once; with SGW_OPT_PAGEABLE_COPY (where the
+  // device reads pageable memory through the host page tables) in ordinary
+  // pages instead, which the filling threads touch first and the kernels read
+  // at their host addresses.  On a GB300 host the 21 GB copy of RMAT-28 took
+  // 1.0-1.08 s to create pinned and 0.47-0.58 s pageable; the plain
+  // schedule's runs took the same time from either (271 ms), the learned
+  // schedule's 4% longer from pageable pages (166 against 160 ms).
   if (g->m > 0) {
     const size_t rec = 4ull * e->W;  // bytes per record in the ends stream
     if (o.transfer_chunk_log2 > 40) return cleanup(fail(SGW_EINVAL, "transfer_chunk_log2 above 40"));
     plan_stream(e->hs_ends, (size_t)e->m * rec, o.transfer_chunk_log2);
     if (e->split) plan_stream(e->hs_w, (size_t)e->m, o.transfer_chunk_log2);
+    if (o.flags & SGW_OPT_PAGEABLE_COPY) {  // where the GPU reads pageable memory through the host page tables
+      int pma = 0, hpt = 0;
+      const bool ok = cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, o.device) == cudaSuccess &&
+                      cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, o.device) ==
+                          cudaSuccess;
+      cudaGetLastError();
+      e->hs_ends.pageable = e->hs_w.pageable = ok && pma && hpt;
+    }
     e->packed_bytes = e->hs_ends.bytes + e->hs_w.bytes;
     HostStream *ends = &e->hs_ends;
     ce = alloc_and_fill(e->hs_ends, e->hs_w, [&](HostStream &hs, size_t k) {
@@ -1507,8 +1540,8 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
     HostStream *streams[2] = {&e->hs_ends, &e->hs_w};
     for (int t = 0; t < 2; ++t)
       for (size_t k = 0; k < streams[t]->h.size(); ++k) {
-        void *dp = nullptr;
-        ce = cudaHostGetDevicePointer(&dp, streams[t]->h[k], 0);
+        void *dp = streams[t]->h[k];  // pageable: the device uses the host address
+        if (!streams[t]->pageable) ce = cudaHostGetDevicePointer(&dp, streams[t]->h[k], 0);
         if (ce != cudaSuccess) {
           cudaGetLastError();
           return cleanup(fail(SGW_ECUDA, "cudaHostGetDevicePointer: %s", cudaGetErrorString(ce)));
@@ -1518,6 +1551,8 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
       }
     ce = cudaMemcpy(e->d_hct, table, sizeof(table), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) return cleanup(fail(SGW_ECUDA, "chunk table upload: %s", cudaGetErrorString(ce)));
+    e->hs_ends.dtab = e->d_hct;
+    e->hs_w.dtab = e->d_hct + kMaxHostChunks;
   }
   e->vec_gather = !(o.flags & SGW_OPT_SCALAR_GATHER) && !e->hs_ends.h.empty();
   if (!allow_gather_smem<false>(kGatherSmemBytes) || !allow_gather_smem<true>(kGatherSmemBytesWide)) {

@@ -882,6 +882,40 @@ __device__ __forceinline__ const char *hc_at(const HostChunks &h, size_t byte) {
   return c + (byte & ((size_t(1) << h.shift) - 1));
 }
 
+// Copies bytes [off, off + bytes) of a host stream to dst, for streams in
+// pageable memory (read through the host page tables), where a DMA copy would
+// be staged by the host thread.  Each thread reads one aligned 16-byte word of
+// the stream (words never straddle chunks) and stores the part in range as
+// one 16-byte word, four 4-byte words or single bytes, whichever the two
+// addresses' alignment allows.  Chunks are padded to 16 bytes, so the words at
+// either end stay inside their chunk.
+__global__ void __launch_bounds__(256) k_copy_host(HostChunks src, unsigned long long off,
+                                                   unsigned long long bytes, uint8_t *__restrict__ dst) {
+  const unsigned long long w0 = off >> 4, w1 = (off + bytes + 15) >> 4, end = off + bytes;
+  const unsigned long long skew = (reinterpret_cast<uintptr_t>(dst) - off) & 15;
+  for (unsigned long long w = w0 + blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; w < w1;
+       w += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long s = w << 4;
+    const uint4 v = *reinterpret_cast<const uint4 *>(hc_at(src, s));
+    if (skew == 0 && s >= off && s + 16 <= end) {
+      *reinterpret_cast<uint4 *>(dst + (s - off)) = v;
+      continue;
+    }
+    const uint32_t q[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const unsigned long long a = s + 4 * k;
+      if ((skew & 3) == 0 && a >= off && a + 4 <= end) {
+        *reinterpret_cast<uint32_t *>(dst + (a - off)) = q[k];
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (a + i >= off && a + i < end) dst[a + i - off] = (uint8_t)(q[k] >> (8 * i));
+      }
+    }
+  }
+}
+
 constexpr int kGatherThreads = 256;
 // Output edges per CTA tile of the vectorised gather (its shared memory is
 // dynamic: 16 bytes per tile edge plus the weight bytes); the scalar gather

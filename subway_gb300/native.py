@@ -26,6 +26,7 @@ OPT_CTA_TILES = 0x10
 OPT_SPLIT_WEIGHTS = 0x20
 OPT_BATCH_PERSISTENT = 0x40
 OPT_BATCH_GRAPH = 0x80
+OPT_PAGEABLE_COPY = 0x100
 SCHED_CAP_COMPACT = 0x1
 SCHED_KEEP_IDLE = 0x2
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}

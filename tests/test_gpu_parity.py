@@ -190,13 +190,15 @@ def test_hub_larger_than_budget(gpu, orc):
             assert np.array_equal(vals, ref), (algo, mode)
 
 
-@pytest.mark.parametrize("flags", ["", "NO_PACK", "SPLIT_WEIGHTS", "SCALAR_GATHER", "NO_PACK|SCALAR_GATHER"])
+@pytest.mark.parametrize("flags", ["", "NO_PACK", "SPLIT_WEIGHTS", "SCALAR_GATHER", "NO_PACK|SCALAR_GATHER",
+                                   "PAGEABLE_COPY", "SPLIT_WEIGHTS|PAGEABLE_COPY", "NO_PACK|PAGEABLE_COPY"])
 def test_transfer_copy_in_small_chunks(gpu, orc, flags):
-    """The host transfer copy cut into dozens of 16 KiB pinned chunks (4 KiB
-    for the hub graph): rows and 16-byte words of the gather, whole-range
-    copies of the learned schedule and the pieces of a vertex larger than
-    the edge buffer all cross chunk boundaries, in every transfer form, and
-    give the oracle's answers."""
+    """The host transfer copy cut into dozens of 16 KiB chunks (4 KiB for the
+    hub graph), pinned or (PAGEABLE_COPY) ordinary pages: rows and 16-byte
+    words of the gather, whole-range copies of the learned schedule and the
+    pieces of a vertex larger than the edge buffer (copy kernel from
+    pageable pages, at 4-byte and byte offsets) all cross chunk boundaries,
+    in every transfer form, and give the oracle's answers."""
     fl = 0
     for f in filter(None, flags.split("|")):
         fl |= getattr(gpu, "OPT_" + f)
