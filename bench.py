@@ -23,9 +23,10 @@ which isolates what the network adds to the schedule's rules.
             sgw_run through the C ABI with host buffers (state init, every
             host->device edge transfer, the distance read-back) and engine
             destruction; the graph load is excluded on both arms.  The engine
-            is made as the drop-in apps make it, with its transfer copy in
-            pageable pages (SGW_OPT_PAGEABLE_COPY: half the set-up time);
-            e2e_pinned is the same with the pinned copy, the library default
+            is made as the drop-in apps make it: no transfer copy, the
+            gather reads the graph's 8-byte records in place through the host
+            page tables (SGW_OPT_GRAPH_IN_PLACE); e2e_pinned is the same with
+            the library default, the packed pinned transfer copy
   e2e_warm  sgw_run alone on a live engine (a resident query service)
 After the timed loops every distinct source's distances from every schedule
 are compared with the OpenMP oracle; the line carries the mismatch count and
@@ -358,9 +359,11 @@ def run_ours(a, dist):
         del eng
 
     # one query as a process runs it: create, run with host buffers, destroy;
-    # the engine made as the drop-in apps make it (transfer copy in pageable
-    # pages), and for the learned schedule also with the pinned copy
-    e2e_loops = [(arm, "e2e", N.OPT_PAGEABLE_COPY) for arm in ("plain", "learned") if arm in arms]
+    # the engine made as the drop-in apps make it (the graph's records read in
+    # place, no transfer copy), and for the learned schedule also with the
+    # library's default pinned copy
+    one_query = N.OPT_GRAPH_IN_PLACE | N.OPT_PAGEABLE_COPY
+    e2e_loops = [(arm, "e2e", one_query) for arm in ("plain", "learned") if arm in arms]
     e2e_loops += [("learned", "e2e_pinned", 0)] if "learned" in arms else []
     for arm, key, xf in e2e_loops:
         walls, st_all = [], []
@@ -375,6 +378,7 @@ def run_ours(a, dist):
                 st_all.append(st)
         res[arm][key + "_walls"] = walls
         res[arm][key + "_reached"] = sum(s["reached_edges"] for s in st_all)
+        res[arm][key + "_h2d"] = sum(s["h2d_bytes"] for s in st_all) / len(st_all)
     refs.clear()
 
     hbm_peak, hbm_src = measured_peaks()
@@ -439,7 +443,7 @@ def run_ours(a, dist):
     e2e_reached = res[head].get("e2e_reached", 0)
     # per e2e step: the node pointers uploaded at engine creation, the edges
     # moved by the run, the distance array read back
-    h2d_e2e = 4 * (g.n + 1) + hs["h2d_bytes_per_run"]
+    h2d_e2e = 4 * (g.n + 1) + res[head].get("e2e_h2d", hs["h2d_bytes_per_run"])
     d2h_e2e = int(sum(s["d2h_bytes"] for s in steps) / K)
     line = {
         "metric": METRIC, "value": hs["value"], "unit": "GTEPS", "n_gpus": dist.world, "steps": K,
@@ -453,7 +457,8 @@ def run_ours(a, dist):
         "e2e": {"value": hs.get("e2e"), "unit": "GTEPS", "h2d_bytes_per_step": int(h2d_e2e),
                 "d2h_bytes_per_step": d2h_e2e, "ms_per_step": hs.get("e2e_ms_per_step"),
                 "includes": "engine creation (arena, transfer copy), sgw_run with host buffers, engine destruction",
-                "transfer_copy": "pageable pages, as the drop-in apps make it (SGW_OPT_PAGEABLE_COPY)"},
+                "transfer_copy": "none: the records read in place, as the drop-in apps do "
+                                 "(SGW_OPT_GRAPH_IN_PLACE)"},
         "e2e_pinned": {"value": hs.get("e2e_pinned"), "unit": "GTEPS", "ms_per_step": hs.get("e2e_pinned_ms_per_step"),
                        "transfer_copy": "pinned (cudaHostAlloc), the library default"},
         "e2e_warm": {"value": hs["e2e_warm"], "unit": "GTEPS", "ms_per_step":

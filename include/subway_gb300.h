@@ -154,6 +154,15 @@ void sgw_graph_free(sgw_graph *g);
  * learned one.  Whole-range and hub copies then run as a copy kernel instead
  * of DMA.  The drop-in apps, which answer one query per process, set it. */
 #define SGW_OPT_PAGEABLE_COPY 0x100u
+/* No transfer copy at all where the device reads pageable memory through the
+ * host page tables and the graph's records are the library's own (from
+ * sgw_graph_load of any format, or the generators; not a file mapping or a
+ * caller's arrays): the gather and copy kernels read the records in place,
+ * at their full size (4 or 8 bytes per edge, not packed or split).  Engine
+ * creation then touches no edge; each run moves up to 8/5 as many bytes as
+ * from the split copy.  Otherwise the flag is ignored (a transfer copy is
+ * made, pageable with SGW_OPT_PAGEABLE_COPY).  The drop-in apps set both. */
+#define SGW_OPT_GRAPH_IN_PLACE 0x200u
 /* sched_flags: the learned policy's inner cap also covers compacted ranges */
 #define SGW_SCHED_CAP_COMPACT 0x1u
 /* sched_flags: transfer active vertices that cannot push, as the reference's
@@ -222,6 +231,9 @@ int sgw_engine_destroy(sgw_engine *e);
 int sgw_engine_max_partition_size(const sgw_engine *e, uint64_t *edges);
 /* Device bytes the engine holds (always <= the budget). */
 int sgw_engine_device_bytes(const sgw_engine *e, uint64_t *bytes);
+/* Bytes of the engine's host transfer copy (0 when it reads the graph's
+ * records in place, SGW_OPT_GRAPH_IN_PLACE). */
+int sgw_engine_host_copy_bytes(const sgw_engine *e, uint64_t *bytes);
 
 typedef struct sgw_run_params {
   int32_t algo;            /* SGW_BFS .. SGW_PR                               */

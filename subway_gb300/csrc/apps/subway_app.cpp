@@ -188,12 +188,10 @@ int main(int argc, char **argv) {
   double t0 = now_ms();
   printf("Reading the input graph from the following file:\n>> %s\n", a.input.c_str());
   sgw_graph *g = nullptr;
-  // binary files are mapped in place (the edges stay in the page cache),
-  // text files parsed
-  const size_t dot = a.input.find_last_of('.');
-  const std::string ext = dot == std::string::npos ? "" : a.input.substr(dot + 1);
-  const bool binary = ext == "bcsr" || ext == "bwcsr" || ext == "bcsr64" || ext == "bwcsr64";
-  int st = binary ? sgw_graph_map(a.input.c_str(), &g) : sgw_graph_load(a.input.c_str(), &g);
+  // every format is read into the library's memory (binary files with
+  // parallel reads, as the reference reads the whole file, text parsed), so
+  // that the engine can gather from the records in place
+  int st = sgw_graph_load(a.input.c_str(), &g);
   if (st != SGW_OK) die(st, "ReadGraph");
   uint32_t n = 0;
   uint64_t m = 0;
@@ -206,7 +204,9 @@ int main(int argc, char **argv) {
   sgw_engine_opts_default(&o);
   o.budget_bytes = a.budget;
   o.device = a.device;
-  o.flags |= SGW_OPT_PAGEABLE_COPY;  // one query per process: the cheaper transfer copy to set up
+  // one query per process: no transfer copy where the GPU reads the records
+  // in place, else the copy that is cheaper to set up
+  o.flags |= SGW_OPT_GRAPH_IN_PLACE | SGW_OPT_PAGEABLE_COPY;
   if (!a.scheduler.empty() && a.budget) sgw_sched_buffers(g, a.budget, &o.num_buffers);
   sgw_engine *e = nullptr;
   st = sgw_engine_create(g, &o, &e);

@@ -57,6 +57,7 @@ struct HostStream {
   uint32_t shift = 30;
   size_t bytes = 0;                    // data bytes
   bool pageable = false;               // chunks are ordinary pages, read through the host page tables
+  bool borrowed = false;               // the graph's own records (not allocated, not freed here)
   const unsigned long long *dtab = nullptr;  // the chunk table on the device
 };
 
@@ -121,6 +122,7 @@ struct sgw_engine {
   size_t packed_bytes = 0;                 // bytes of the whole transfer copy
 
   bool vec_gather = false;                 // host records readable as aligned 16-B words
+  bool in_place = false;                   // the gather reads the graph's own records (no transfer copy)
   uint32_t cur_streamed = 0;               // partition being relaxed: whole-range buffer
   uint64_t cur_stream_base = 0;            //   and the first edge of that range
   uint32_t pbits = 0;                      // packed: bits of the destination id
@@ -318,7 +320,7 @@ cudaError_t alloc_and_fill(HostStream &a, HostStream &b, Fill fill) {
 void free_streams(HostStream &a, HostStream &b) {
   std::vector<std::pair<char *, size_t>> all;  // (chunk, bytes if pageable else 0)
   for (HostStream *hs : {&a, &b})
-    for (size_t k = 0; k < hs->h.size(); ++k)
+    for (size_t k = 0; k < hs->h.size() && !hs->borrowed; ++k)
       if (hs->h[k]) all.push_back({hs->h[k], hs->pageable ? hs->size[k] : 0});
   auto work = [&](size_t t) {
     for (size_t i = t; i < all.size(); i += 2) {
@@ -1421,14 +1423,33 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
       return fail(SGW_ERANGE, "a 4096-vertex tile holds 2^31 edges or more");
     }
   }
+  // whether the device reads pageable memory through the host page tables
+  bool pageable_ok = false;
+  if (o.flags & (SGW_OPT_PAGEABLE_COPY | SGW_OPT_GRAPH_IN_PLACE)) {
+    int pma = 0, hpt = 0;
+    pageable_ok = cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, o.device) == cudaSuccess &&
+                  cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, o.device) ==
+                      cudaSuccess && pma && hpt;
+    cudaGetLastError();
+  }
+  // In place: records the library itself holds in anonymous memory (loaded
+  // or generated; 64 KiB aligned and rounded up, so the 16-byte words the
+  // gather reads past the last record stay inside the allocation).  File
+  // mappings and caller arrays get a transfer copy.
+  {
+    const size_t rec_bytes = size_t(g->m) * g->esz;
+    e->in_place = (o.flags & SGW_OPT_GRAPH_IN_PLACE) && pageable_ok && g->owns && !g->map_base && g->m > 0 &&
+                  ((uintptr_t)g->edges & 15u) == 0 && g->edges_bytes_alloc >= rec_bytes + 16;
+  }
   // weighted records travel as one packed word when (w << bits(n)) | dst fits
   const uint32_t wmax = max_weight(g);  // one pass over the records
-  bool pack = g->weighted && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SPLIT_WEIGHTS)) &&
+  bool pack = !e->in_place && g->weighted && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SPLIT_WEIGHTS)) &&
               pack_bits_for(g, wmax, &e->pbits);
   if (pack) e->W = 1;
   else e->pbits = 0;
   // otherwise weights below 256 travel as their own byte stream
-  e->split = g->weighted && !pack && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SCALAR_GATHER)) && wmax < 256;
+  e->split = !e->in_place && g->weighted && !pack && !(o.flags & (SGW_OPT_NO_PACK | SGW_OPT_SCALAR_GATHER)) &&
+             wmax < 256;
   if (e->split) e->W = 1;
   e->rec_bytes = 4 * e->W + (e->split ? 1 : 0);
   e->nbuf = (o.flags & SGW_OPT_NO_OVERLAP) ? 1 : 2;
@@ -1498,19 +1519,21 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
   // 1.0-1.08 s to create pinned and 0.47-0.58 s pageable; the plain
   // schedule's runs took the same time from either (271 ms), the learned
   // schedule's 4% longer from pageable pages (166 against 160 ms).
-  if (g->m > 0) {
+  if (g->m > 0 && e->in_place) {  // one borrowed chunk: the graph's records
+    HostStream &hs = e->hs_ends;
+    hs.bytes = (size_t)e->m * g->esz;
+    hs.shift = 62;
+    hs.h.assign(1, static_cast<char *>(g->edges));
+    hs.d.assign(1, 0);
+    hs.size.assign(1, g->edges_bytes_alloc);
+    hs.pageable = hs.borrowed = true;
+    e->packed_bytes = 0;
+  } else if (g->m > 0) {
     const size_t rec = 4ull * e->W;  // bytes per record in the ends stream
     if (o.transfer_chunk_log2 > 40) return cleanup(fail(SGW_EINVAL, "transfer_chunk_log2 above 40"));
     plan_stream(e->hs_ends, (size_t)e->m * rec, o.transfer_chunk_log2);
     if (e->split) plan_stream(e->hs_w, (size_t)e->m, o.transfer_chunk_log2);
-    if (o.flags & SGW_OPT_PAGEABLE_COPY) {  // where the GPU reads pageable memory through the host page tables
-      int pma = 0, hpt = 0;
-      const bool ok = cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, o.device) == cudaSuccess &&
-                      cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, o.device) ==
-                          cudaSuccess;
-      cudaGetLastError();
-      e->hs_ends.pageable = e->hs_w.pageable = ok && pma && hpt;
-    }
+    e->hs_ends.pageable = e->hs_w.pageable = (o.flags & SGW_OPT_PAGEABLE_COPY) && pageable_ok;
     e->packed_bytes = e->hs_ends.bytes + e->hs_w.bytes;
     HostStream *ends = &e->hs_ends;
     ce = alloc_and_fill(e->hs_ends, e->hs_w, [&](HostStream &hs, size_t k) {
@@ -1536,6 +1559,8 @@ int sgw_engine_create(const sgw_graph *g, const sgw_engine_opts *opts_in, sgw_en
       return cleanup(fail(SGW_ECUDA, "cudaHostAlloc of the %zu-byte transfer copy: %s", e->packed_bytes,
                           cudaGetErrorString(ce)));
     }
+  }
+  if (g->m > 0) {  // chunk tables: device addresses (pageable and borrowed chunks: the host address)
     unsigned long long table[2 * kMaxHostChunks] = {};
     HostStream *streams[2] = {&e->hs_ends, &e->hs_w};
     for (int t = 0; t < 2; ++t)
@@ -1621,6 +1646,12 @@ int sgw_engine_destroy(sgw_engine *e) {
 int sgw_engine_max_partition_size(const sgw_engine *e, uint64_t *edges) {
   if (!e || !edges) return fail(SGW_EINVAL, "null argument");
   *edges = e->cap;
+  return SGW_OK;
+}
+
+int sgw_engine_host_copy_bytes(const sgw_engine *e, uint64_t *bytes) {
+  if (!e || !bytes) return fail(SGW_EINVAL, "null argument");
+  *bytes = e->packed_bytes;
   return SGW_OK;
 }
 

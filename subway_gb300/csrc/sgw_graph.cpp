@@ -62,7 +62,8 @@ int graph_alloc(uint32_t n, uint64_t m, int weighted, sgw_graph **out) {
   void *np = host_alloc((wide ? 8 : 4) * (size_t(n) + 1), nullptr);
   if (wide) g->node_pointer64 = (uint64_t *)np;
   else g->node_pointer = (uint32_t *)np;
-  g->edges = host_alloc(size_t(m) * g->esz, &g->edges_bytes_alloc);
+  // 16 spare bytes: the engine's 16-byte reads of the last records stay inside
+  g->edges = host_alloc(size_t(m) * g->esz + 16, &g->edges_bytes_alloc);
   if (!np || !g->edges) {
     host_free(np);
     host_free(g->edges);

@@ -27,6 +27,7 @@ OPT_SPLIT_WEIGHTS = 0x20
 OPT_BATCH_PERSISTENT = 0x40
 OPT_BATCH_GRAPH = 0x80
 OPT_PAGEABLE_COPY = 0x100
+OPT_GRAPH_IN_PLACE = 0x200
 SCHED_CAP_COMPACT = 0x1
 SCHED_KEEP_IDLE = 0x2
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
@@ -88,6 +89,7 @@ _PROTOS = {
     "sgw_engine_destroy": (C.c_int, [_P]),
     "sgw_engine_max_partition_size": (C.c_int, [_P, _u64p]),
     "sgw_engine_device_bytes": (C.c_int, [_P, _u64p]),
+    "sgw_engine_host_copy_bytes": (C.c_int, [_P, _u64p]),
     "sgw_run_params_default": (None, [C.POINTER(RunParams), C.c_int, C.c_int, C.c_uint32]),
     "sgw_run": (C.c_int, [_P, C.POINTER(RunParams), _P, C.POINTER(RunStats)]),
     "sgw_state_init": (C.c_int, [_P, C.POINTER(RunParams)]),
@@ -357,6 +359,12 @@ class Engine:
     def device_bytes(self) -> int:
         v = C.c_uint64()
         check(lib().sgw_engine_device_bytes(self.h, C.byref(v)), "device_bytes")
+        return v.value
+
+    def host_copy_bytes(self) -> int:
+        """Bytes of the host transfer copy (0 when the records are read in place)."""
+        v = C.c_uint64()
+        check(lib().sgw_engine_host_copy_bytes(self.h, C.byref(v)), "host_copy_bytes")
         return v.value
 
     def dma_rate(self) -> float:

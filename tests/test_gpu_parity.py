@@ -450,3 +450,67 @@ def test_odd_vertex_counts(gpu, orc, n):
             for mode in MODES:
                 vals, _ = eng.run(algo, mode, s0)
                 assert np.array_equal(vals, _oracle(orc, g, algo, s0)), (n, policy, algo, mode)
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_graph_read_in_place(gpu, orc, tmp_path, weighted):
+    """SGW_OPT_GRAPH_IN_PLACE: on records the library holds (generated or
+    loaded) the engine makes no transfer copy and gathers, streams and
+    copies hub pieces from the records themselves through the host page
+    tables; a caller's arrays still get a (pageable) copy.  Every answer is
+    the oracle's, plain and learned, with hubs larger than the buffer."""
+    fl = gpu.OPT_GRAPH_IN_PLACE | gpu.OPT_PAGEABLE_COPY
+    g = gpu.Graph.rmat(14, 16, seed=12, weighted=weighted, wmax=64)
+    ext = "bwcsr" if weighted else "bcsr"
+    g.save(tmp_path / f"g.{ext}")
+    loaded = gpu.Graph.load(tmp_path / f"g.{ext}")
+    budget = 18 * g.n + 128 * 1024 + (g.m // 6) * 8 * 3
+    src = int(g.pick_sources(1, seed=3)[0])
+    algos = ("bfs", "sssp", "sswp", "cc") if weighted else ("bfs", "cc")
+    for graph in (g, loaded):
+        plain = gpu.Engine(graph, budget_bytes=budget, flags=fl)
+        learned = gpu.Engine(graph, budget_bytes=budget, flags=fl, num_buffers=3)
+        learned.set_policy("learned")
+        assert plain.host_copy_bytes() == 0 and learned.host_copy_bytes() == 0
+        assert plain.max_partition_size() < graph.m
+        for algo in algos:
+            ref = _oracle(orc, graph, algo, src)
+            for mode in MODES:
+                for eng in (plain, learned):
+                    vals, _ = eng.run(algo, mode, src)
+                    assert np.array_equal(vals, ref), (algo, mode)
+        plain.close()
+        learned.close()
+    caller = gpu.Graph.from_csr(np.array(g.node_pointer), np.array(g.edges), weighted)
+    e = gpu.Engine(caller, budget_bytes=budget, flags=fl)
+    assert e.host_copy_bytes() > 0
+    vals, _ = e.run("bfs", "async", src)
+    assert np.array_equal(vals, _oracle(orc, caller, "bfs", src))
+    e.close()
+    # a vertex above the edge buffer, streamed in pieces from the records
+    n = 3000
+    rng = np.random.default_rng(9)
+    hs = np.concatenate([np.zeros(2500, np.int64), rng.integers(0, n, 4000)])
+    hd = np.concatenate([np.arange(1, 2501), rng.integers(0, n, 4000)])
+    keep = (hs != hd) & (hs != n - 2)
+    pairs = np.unique(np.stack([hs[keep], hd[keep]], 1), axis=0)
+    npt = np.zeros(n + 1, np.uint32)
+    np.add.at(npt, pairs[:, 0] + 1, 1)
+    npt = np.cumsum(npt).astype(np.uint32)
+    w = (1 + (pairs[:, 0] * 7 + pairs[:, 1] * 13) % 50).astype(np.uint32)
+    hub = gpu.Graph.from_csr(npt, np.stack([pairs[:, 1].astype(np.uint32), w], 1), True)
+    hub.save(tmp_path / "hub.bwcsr")
+    hub = gpu.Graph.load(tmp_path / "hub.bwcsr")
+    heng = None
+    for extra in range(0, 64 * 1024, 1024):  # the smallest budget the 8-byte records fit
+        try:
+            heng = gpu.Engine(hub, budget_bytes=18 * n + 13 * 1024 + 1000 * 16 + extra, flags=fl)
+            break
+        except gpu.SgwError:
+            continue
+    assert heng is not None and heng.host_copy_bytes() == 0 and heng.max_partition_size() < 2500
+    for algo in ("bfs", "sssp", "sswp", "cc"):
+        for mode in MODES:
+            vals, _ = heng.run(algo, mode, 0)
+            assert np.array_equal(vals, _oracle(orc, hub, algo, 0)), (algo, mode)
+    heng.close()
