@@ -366,17 +366,22 @@ def run_ours(a, dist):
     e2e_loops = [(arm, "e2e", one_query) for arm in ("plain", "learned") if arm in arms]
     e2e_loops += [("learned", "e2e_pinned", 0)] if "learned" in arms else []
     for arm, key, xf in e2e_loops:
-        walls, st_all = [], []
+        walls, st_all, phases = [], [], []
         for k in range(a.warmup + a.steps):
             t = time.perf_counter()
             eng = make_engine(arm, xf)
+            t1 = time.perf_counter()
             _, st = eng.run(a.algo, a.mode, sources[k % len(sources)], out=out)
+            t2 = time.perf_counter()
             eng.close()
-            w = time.perf_counter() - t
+            t3 = time.perf_counter()
             if k >= a.warmup:
-                walls.append(w)
+                walls.append(t3 - t)
                 st_all.append(st)
+                phases.append((t1 - t, t2 - t1, t3 - t2))
         res[arm][key + "_walls"] = walls
+        res[arm][key + "_phases_ms"] = {name: round(1e3 * sum(p[i] for p in phases) / len(phases), 2)
+                                        for i, name in enumerate(("create", "run", "destroy"))}
         res[arm][key + "_reached"] = sum(s["reached_edges"] for s in st_all)
         res[arm][key + "_h2d"] = sum(s["h2d_bytes"] for s in st_all) / len(st_all)
     refs.clear()
@@ -458,8 +463,10 @@ def run_ours(a, dist):
                 "d2h_bytes_per_step": d2h_e2e, "ms_per_step": hs.get("e2e_ms_per_step"),
                 "includes": "engine creation (arena, transfer copy), sgw_run with host buffers, engine destruction",
                 "transfer_copy": "none: the records read in place, as the drop-in apps do "
-                                 "(SGW_OPT_GRAPH_IN_PLACE)"},
+                                 "(SGW_OPT_GRAPH_IN_PLACE)",
+                "phases_ms": res[head].get("e2e_phases_ms")},
         "e2e_pinned": {"value": hs.get("e2e_pinned"), "unit": "GTEPS", "ms_per_step": hs.get("e2e_pinned_ms_per_step"),
+                       "phases_ms": res[head].get("e2e_pinned_phases_ms"),
                        "transfer_copy": "pinned (cudaHostAlloc), the library default"},
         "e2e_warm": {"value": hs["e2e_warm"], "unit": "GTEPS", "ms_per_step":
                      round(dist.max(sum(s["wall_ms"] for s in steps)) / K, 4)},
