@@ -116,6 +116,13 @@ int sgw_graph_out_degree(const sgw_graph *g, uint32_t *out_degree);
  * .bwcsr64, or .el/.wel text, chosen by extension; SGW_ERANGE for a u32
  * file of a graph with 2^32 edges or more. */
 int sgw_graph_save(const sgw_graph *g, const char *path);
+/* Removes vertex v's out-edges (the rows after it move down, m shrinks; the
+ * node pointers keep their width).  Only for a graph whose arrays the library
+ * owns (sgw_graph_load, the generators), and not while an engine or batch
+ * uses it.  The apps' --subway-compat uses it on vertex n - 2, whose
+ * out-degree the reference never writes (shared/graph.cu:179-181), so that
+ * its edges are ignored there. */
+int sgw_graph_clear_out_edges(sgw_graph *g, uint32_t v);
 void sgw_graph_free(sgw_graph *g);
 
 /* ---- engine --------------------------------------------------------------- */
@@ -341,6 +348,11 @@ int sgw_trace_enable(sgw_engine *e, int on);
 int sgw_trace_count(const sgw_engine *e, uint64_t *count);
 int sgw_trace_read(const sgw_engine *e, sgw_trace_rec *out, uint64_t capacity,
                    uint64_t *count);
+/* The trace as a CSV file (a header line, then one line per record, the
+ * fields in struct order; `reserved` left out).  sgw_trace_save writes the
+ * engine's records; sgw_trace_write_csv any array of them. */
+int sgw_trace_save(const sgw_engine *e, const char *path);
+int sgw_trace_write_csv(const sgw_trace_rec *recs, uint64_t count, const char *path);
 
 /* Partition planning on the host: the greedy split of a compacted active
  * queue (prefix array ptr of count+1 entries) into runs whose edge count is

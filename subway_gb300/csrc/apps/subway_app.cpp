@@ -12,7 +12,10 @@
 // --scheduler MODEL (learned scheduling policy with this network file; the
 // answers are the same, the schedule and the bytes moved change), --precision
 // DIGITS (significant digits of PageRank values in the --output file; the
-// reference writes 6, 9 round-trips every float exactly).
+// reference writes 6, 9 round-trips every float exactly), --trace FILE (the
+// per-partition trace as CSV), --subway-compat 1 (vertex n-2's out-edges
+// ignored, as the reference ignores them: it never writes that vertex's
+// out-degree, shared/graph.cu:179-181).
 //
 // Invoked as `converter`, it is the reference's tools/converter: one argument,
 // a .el or .wel file, written beside it as .bcsr or .bwcsr (.bcsr64 / .bwcsr64
@@ -33,7 +36,8 @@
 namespace {
 
 struct Args {
-  std::string input, output, stats, scheduler;
+  std::string input, output, stats, scheduler, trace;
+  bool compat = false;
   unsigned source = 0;
   int device = 0;
   unsigned long long budget = 0;
@@ -54,6 +58,8 @@ std::string help(bool can_source) {
   s += "\n    [--stats]: Write run statistics as JSON to this file";
   s += "\n    [--scheduler]: Learned scheduling with this model file (e.g. subway_gb300/models/sched_mlp.bin)";
   s += "\n    [--precision]: Significant digits of float results in the output file (default: 6)";
+  s += "\n    [--trace]: Write the per-partition trace as CSV to this file";
+  s += "\n    [--subway-compat]: 1 = ignore vertex n-2's out-edges, as the reference does";
   s += "\n\n";
   return s;
 }
@@ -83,6 +89,8 @@ Args parse(int argc, char **argv, bool can_source) {
     else if (!strcmp(k, "--stats")) a.stats = v;
     else if (!strcmp(k, "--scheduler")) a.scheduler = v;
     else if (!strcmp(k, "--precision")) a.precision = std::max(1, std::min(17, atoi(v)));
+    else if (!strcmp(k, "--trace")) a.trace = v;
+    else if (!strcmp(k, "--subway-compat")) a.compat = atoi(v) != 0;
     else {
       std::string m = std::string("\nThere was an error parsing command line argument <") + k + ">\n";
       usage_exit(can_source, m.c_str());
@@ -193,6 +201,11 @@ int main(int argc, char **argv) {
   // that the engine can gather from the records in place
   int st = sgw_graph_load(a.input.c_str(), &g);
   if (st != SGW_OK) die(st, "ReadGraph");
+  if (a.compat) {
+    uint32_t nn = 0;
+    sgw_graph_info64(g, &nn, nullptr, nullptr);
+    if (nn >= 2 && (st = sgw_graph_clear_out_edges(g, nn - 2)) != SGW_OK) die(st, "subway-compat");
+  }
   uint32_t n = 0;
   uint64_t m = 0;
   int weighted = 0;
@@ -265,6 +278,7 @@ int main(int argc, char **argv) {
     if (algo == SGW_PR) save_f32(a.output, vf, a.precision);
     else save_u32(a.output, vu);
   }
+  if (!a.trace.empty() && (st = sgw_trace_save(e, a.trace.c_str())) != SGW_OK) die(st, "trace");
   if (!a.stats.empty()) {
     FILE *f = fopen(a.stats.c_str(), "w");
     if (f) {

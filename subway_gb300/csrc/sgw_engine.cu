@@ -1798,6 +1798,11 @@ int sgw_trace_read(const sgw_engine *e, sgw_trace_rec *out, uint64_t capacity, u
   return SGW_OK;
 }
 
+int sgw_trace_save(const sgw_engine *e, const char *path) {
+  if (!e) return fail(SGW_EINVAL, "null engine");
+  return sgw_trace_write_csv(e->trace.data(), e->trace.size(), path);
+}
+
 int sgw_read_values(sgw_engine *e, void *out_values) {
   clear_error();
   if (!e || !out_values) return fail(SGW_EINVAL, "null argument");

@@ -937,6 +937,42 @@ int sgw_graph_save(const sgw_graph *g, const char *path) {
   return ok ? SGW_OK : fail(SGW_EIO, "write failed for %s", path);
 }
 
+int sgw_graph_clear_out_edges(sgw_graph *g, uint32_t v) {
+  clear_error();
+  if (!g) return fail(SGW_EINVAL, "null graph");
+  if (v >= g->n) return fail(SGW_EINVAL, "vertex %u out of range (n=%u)", v, g->n);
+  if (!g->owns || g->map_base)
+    return fail(SGW_EINVAL, "only a graph whose arrays the library owns (loaded or generated) can be changed");
+  const uint64_t a = np_at(g, v), b = np_at(g, uint64_t(v) + 1), d = b - a;
+  if (d == 0) return SGW_OK;
+  char *ed = static_cast<char *>(g->edges);
+  memmove(ed + a * g->esz, ed + b * g->esz, size_t(g->m - b) * g->esz);
+#pragma omp parallel for
+  for (int64_t u = (int64_t)v + 1; u <= (int64_t)g->n; ++u) np_set(g, (uint64_t)u, np_at(g, (uint64_t)u) - d);
+  g->m -= d;
+  g->wmax_cache.store(-1, std::memory_order_relaxed);
+  return SGW_OK;
+}
+
+int sgw_trace_write_csv(const sgw_trace_rec *recs, uint64_t count, const char *path) {
+  clear_error();
+  if (!path || (count && !recs)) return fail(SGW_EINVAL, "null argument");
+  FILE *f = fopen(path, "w");
+  if (!f) return fail(SGW_EIO, "cannot create %s", path);
+  bool ok = fprintf(f, "global_iteration,partition,num_partitions,inner_iterations,active_nodes,first_vertex,"
+                       "active_edges,iteration_active_nodes,iteration_active_edges,bytes_h2d,transfer\n") > 0;
+  for (uint64_t i = 0; ok && i < count; ++i) {
+    const sgw_trace_rec &r = recs[i];
+    ok = fprintf(f, "%u,%u,%u,%u,%u,%u,%llu,%llu,%llu,%llu,%u\n", r.global_iteration, r.partition,
+                 r.num_partitions, r.inner_iterations, r.active_nodes, r.first_vertex,
+                 (unsigned long long)r.active_edges, (unsigned long long)r.iteration_active_nodes,
+                 (unsigned long long)r.iteration_active_edges, (unsigned long long)r.bytes_h2d,
+                 r.transfer) > 0;
+  }
+  if (fclose(f) != 0) ok = false;
+  return ok ? SGW_OK : fail(SGW_EIO, "write failed for %s", path);
+}
+
 void sgw_graph_free(sgw_graph *g) {
   if (!g) return;
   if (g->map_base) {

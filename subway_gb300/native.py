@@ -130,6 +130,9 @@ _PROTOS = {
     "sgw_trace_enable": (C.c_int, [_P, C.c_int]),
     "sgw_trace_count": (C.c_int, [_P, _u64p]),
     "sgw_trace_read": (C.c_int, [_P, _P, C.c_uint64, _u64p]),
+    "sgw_trace_save": (C.c_int, [_P, C.c_char_p]),
+    "sgw_trace_write_csv": (C.c_int, [_P, C.c_uint64, C.c_char_p]),
+    "sgw_graph_clear_out_edges": (C.c_int, [_P, C.c_uint32]),
     "sgw_gen_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
                                C.c_uint64, C.c_int, C.c_uint32, C.POINTER(_P)]),
     "sgw_gen_er": (C.c_int, [C.c_uint32, C.c_uint64, C.c_uint64, C.c_int, C.c_uint32, C.POINTER(_P)]),
@@ -282,6 +285,13 @@ class Graph:
 
     def save(self, path):
         check(lib().sgw_graph_save(self.h, str(path).encode()), f"sgw_graph_save({path})")
+
+    def clear_out_edges(self, v):
+        """Removes vertex v's out-edges (graphs the library owns only)."""
+        check(lib().sgw_graph_clear_out_edges(self.h, int(v)), "sgw_graph_clear_out_edges")
+        n, m = C.c_uint32(), C.c_uint64()
+        check(lib().sgw_graph_info64(self.h, C.byref(n), C.byref(m), None), "sgw_graph_info64")
+        self.m = m.value
 
     def symmetrize(self) -> "Graph":
         h = _P()
@@ -442,6 +452,20 @@ class Engine:
 POLICY_PLAIN, POLICY_LEARNED = 0, 1
 MLP_INPUTS, MLP_PARAMS = 5, 4609
 ACT_SKIP, ACT_RESIDENT, ACT_STREAM, ACT_COMPACT, ACT_SPLIT = 0, 1, 2, 3, 4
+
+TRACE_REC = np.dtype([("global_iteration", "<u4"), ("partition", "<u4"), ("num_partitions", "<u4"),
+                      ("inner_iterations", "<u4"), ("active_nodes", "<u4"), ("first_vertex", "<u4"),
+                      ("active_edges", "<u8"), ("iteration_active_nodes", "<u8"),
+                      ("iteration_active_edges", "<u8"), ("bytes_h2d", "<u8"), ("transfer", "<u4"),
+                      ("reserved", "<u4")])
+
+
+def write_trace_csv(recs: np.ndarray, path):
+    """sgw_trace_write_csv over an array of TRACE_REC records."""
+    r = np.ascontiguousarray(recs, dtype=TRACE_REC)
+    check(lib().sgw_trace_write_csv(r.ctypes.data if len(r) else None, len(r), str(path).encode()),
+          "sgw_trace_write_csv")
+
 
 RANGE_REC = np.dtype([("global_iteration", "<u4"), ("range", "<u4"), ("active_nodes", "<u4"),
                       ("range_nodes", "<u4"), ("active_edges", "<u4"), ("range_edges", "<u4"),

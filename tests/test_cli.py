@@ -159,3 +159,32 @@ def test_pr_output_precision(gpu, orc, bindir, tmp_path):
             assert all(f"{float(v):.9g}" == s for v, s in zip(x, vals))
         ref, _ = orc.pagerank(g.node_pointer, g.ends)
         assert np.max(np.abs(x - ref) / ref) < 1e-4
+
+
+@pytest.mark.gpu
+def test_app_subway_compat_and_trace(gpu, orc, bindir, tmp_path):
+    """--subway-compat 1 ignores vertex n-2's out-edges as the reference does
+    (it never writes that out-degree, shared/graph.cu:179-181); without it
+    they count.  --trace writes one CSV line per processed partition."""
+    n = 3000
+    rng = np.random.default_rng(11)
+    deg = rng.integers(1, 8, n)
+    deg[n - 2] = 60  # vertex n - 2 reaches much of the graph
+    npt = np.concatenate([[0], np.cumsum(deg)]).astype(np.uint32)
+    dst = rng.integers(0, n, int(npt[-1])).astype(np.uint32)
+    path = tmp_path / "g.bcsr"
+    gpu.Graph.from_csr(npt, dst, False).save(path)
+    cut = np.concatenate([dst[:npt[n - 2]], dst[npt[n - 1]:]])
+    npc = npt.astype(np.int64).copy()
+    npc[n - 1:] -= deg[n - 2]
+    src = n - 2
+    for compat, (p_, e_) in ((0, (npt, dst)), (1, (npc.astype(np.uint32), cut))):
+        out, trace = tmp_path / f"out{compat}.txt", tmp_path / f"trace{compat}.csv"
+        p = _run(bindir, "bfs-async", "--input", path, "--output", out, "--source", src, "--trace", trace,
+                 "--subway-compat", compat, "--budget", 18 * n + 64 * 1024 + 2000 * 8)
+        assert p.returncode == 0, p.stderr
+        rows = np.loadtxt(out)
+        assert np.array_equal(rows[:, 1].astype(np.uint64), orc.run("bfs", p_, e_, src).astype(np.uint64)), compat
+        lines = trace.read_text().splitlines()
+        assert lines[0].startswith("global_iteration,partition,") and len(lines) >= 2
+        assert all(len(x.split(",")) == 11 for x in lines[1:])
