@@ -214,11 +214,12 @@ typedef struct sgw_engine_opts {
    * 2^transfer_chunk_log2 bytes (0 = 30, i.e. 1 GiB; at most 64 chunks per
    * stream, larger chunks if needed), two chunks at a time. */
   uint32_t transfer_chunk_log2;
-  /* Most edges one generate queues (BFS/SSSP/SSWP/CC): the active vertices
-   * of whole 4096-vertex tiles, in vertex order, up to this many edges (the
-   * first tile with edges always); the rest stay active for the next
-   * iteration, which the answers do not depend on.  0 = 2^31 for graphs of
-   * 2^32 edges or more (queue positions are u32), else no limit. */
+  /* Most edges one generate queues: the active vertices of whole 4096-vertex
+   * tiles, in vertex order, up to this many edges (the first tile with edges
+   * always); the rest stay active for the next iteration, which the
+   * BFS/SSSP/SSWP/CC answers do not depend on (PageRank keeps their
+   * residuals for the next round).  0 = 2^31 for graphs of 2^32 edges or
+   * more (queue positions are u32), else no limit. */
   uint32_t generate_edge_limit;
 } sgw_engine_opts;
 

@@ -590,7 +590,7 @@ int launch_generate(sgw_engine *e, int consume) {
   a.epoch = e->epoch;
   a.num_tiles = e->num_tiles;
   a.consume = consume;
-  a.edge_limit = e->fam == FAM_INT ? e->edge_limit : 0u;
+  a.edge_limit = e->edge_limit;
   a.delta = e->d_delta;
   a.pval = e->d_pval;
   a.qpush = e->d_qpush;
@@ -612,17 +612,14 @@ int launch_generate(sgw_engine *e, int consume) {
   CK(cudaMemsetAsync(&e->d_ctl->num_seen, 0, sizeof(uint32_t), e->s_comp));
   size_t slot = 0;
   TRY(prof_begin(e, K_GENERATE, e->s_comp, &slot));
-  if (e->fam == FAM_PR) {
-    k_generate<true><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
-    e->stats.launches += 1;
-  } else {
-    k_generate_count<<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
-    CK(cudaGetLastError());
-    k_generate_scan<<<1, kGenScanThreads, 0, e->s_comp>>>(a);
-    CK(cudaGetLastError());
-    k_generate_write<<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
-    e->stats.launches += 3;
-  }
+  if (e->fam == FAM_PR) k_generate_count<true><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  else k_generate_count<false><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  CK(cudaGetLastError());
+  k_generate_scan<<<1, kGenScanThreads, 0, e->s_comp>>>(a);
+  CK(cudaGetLastError());
+  if (e->fam == FAM_PR) k_generate_write<true><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  else k_generate_write<false><<<e->num_tiles, kGenThreads, 0, e->s_comp>>>(a);
+  e->stats.launches += 3;
   CK(cudaGetLastError());
   TRY(prof_end(e, e->s_comp, slot));
   e->stats.generate_launches += 1;
@@ -972,8 +969,6 @@ int validate_params(const sgw_engine *e, const sgw_run_params *p) {
     return fail(SGW_EBUDGET, "budget too small for the PageRank vertex state (f64 ranks and residuals)");
   if (p->algo == SGW_PR && !(p->pr_acc > 0.0f) )
     return fail(SGW_EINVAL, "pr_acc must be positive");
-  if (p->algo == SGW_PR && e->m >= (uint64_t(1) << 32))  // its generate has no edge limit
-    return fail(SGW_ERANGE, "PageRank needs fewer than 2^32 edges");
   if ((p->algo == SGW_SSSP || p->algo == SGW_SSWP) && !e->g->weighted)
     return fail(SGW_EINVAL, "SSSP/SSWP need a weighted graph (.bwcsr/.wel)");
   if (p->algo != SGW_CC && p->algo != SGW_PR && p->source >= e->n)

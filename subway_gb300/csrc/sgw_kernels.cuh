@@ -479,6 +479,52 @@ __device__ __forceinline__ void gen_lane(const GenArgs &a, uint32_t v0, bool ful
   }
 }
 
+// PageRank selection for the lane's 16 vertices (prePrefix PR overload,
+// shared/subgraph_generator.cu:24-41): active = delta > acc.  keepmask: the
+// active vertices with out-edges (queued); clearmask: every active vertex,
+// whose residual the write pass moves into its rank.  Reads only.
+__device__ __forceinline__ void gen_lane_pr(const GenArgs &a, uint32_t v0, bool full, GenLane &L) {
+  double dl[kGenVPerLane];
+  if (full) {
+#pragma unroll
+    for (int q = 0; q < kGenVPerLane / 2; ++q) {
+      const double2 p = reinterpret_cast<const double2 *>(a.delta + v0)[q];
+      dl[2 * q] = p.x;
+      dl[2 * q + 1] = p.y;
+    }
+  } else {
+#pragma unroll
+    for (uint32_t k = 0; k < kGenVPerLane; ++k) dl[k] = v0 + k < a.n ? a.delta[v0 + k] : 0.0;
+  }
+  uint32_t actmask = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kGenVPerLane; ++k)
+    if (dl[k] > a.acc) actmask |= 1u << k;
+  L.seen = (uint32_t)__popc(actmask);
+  L.clearmask = actmask;
+  if (!actmask) return;
+  if (full) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint4 p = __ldg(reinterpret_cast<const uint4 *>(a.off + v0) + q);
+      L.o[4 * q] = p.x; L.o[4 * q + 1] = p.y; L.o[4 * q + 2] = p.z; L.o[4 * q + 3] = p.w;
+    }
+    L.o[kGenVPerLane] = __ldg(&a.off[v0 + kGenVPerLane]);
+  } else {
+#pragma unroll
+    for (uint32_t k = 0; k <= kGenVPerLane; ++k) L.o[k] = (v0 + k <= a.n) ? __ldg(&a.off[v0 + k]) : 0u;
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < kGenVPerLane; ++k) {
+    const uint32_t d = L.o[k + 1] - L.o[k];
+    if (((actmask >> k) & 1u) && d) {
+      L.keepmask |= 1u << k;
+      ++L.cnt;
+      L.edges += d;
+    }
+  }
+}
+
 // Clears the labels of the lane's vertices in L.clearmask (16-byte stores of
 // the words read by gen_lane when the group is whole).
 __device__ __forceinline__ void gen_clear(const GenArgs &a, uint32_t v0, bool full, const GenLane &L) {
@@ -506,6 +552,7 @@ __device__ __forceinline__ void gen_clear(const GenArgs &a, uint32_t v0, bool fu
 // clear bits it records per group (so the write pass reads 4 bytes per 16
 // vertices instead of the labels and values again), the label clearing, and
 // the tile's (count, edges) total.
+template <bool PR>
 __global__ void __launch_bounds__(kGenThreads) k_generate_count(GenArgs a) {
   __shared__ unsigned long long s_warp[kGenThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -514,8 +561,12 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_count(GenArgs a) {
   const bool full = v0 + kGenVPerLane <= a.n;
   GenLane L;
   if (v0 < a.n) {
-    gen_lane(a, v0, full, L);
-    if (!a.edge_limit) gen_clear(a, v0, full, L);
+    if (PR) {
+      gen_lane_pr(a, v0, full, L);  // residuals move in the write pass
+    } else {
+      gen_lane(a, v0, full, L);
+      if (!a.edge_limit) gen_clear(a, v0, full, L);
+    }
     a.gmask[v0 / kGenVPerLane] = L.keepmask | (L.clearmask << 16);
   }
   const uint32_t seen = __reduce_add_sync(0xffffffffu, L.seen);
@@ -649,7 +700,12 @@ __global__ void __launch_bounds__(kGenScanThreads) k_generate_scan(GenArgs a) {
 }
 
 // Write pass: the group's keep bits from the count pass, the node pointers
-// of groups that queue a vertex, and the queue / pointer entries.
+// of groups that queue a vertex, and the queue / pointer entries.  PR: every
+// active vertex's residual moves into its rank (value += delta, delta = 0,
+// the first half of pr_kernel, shared/gpu_kernels.cu:234-250) and its queue
+// entry carries the push damping * delta / outdeg, so each round is a
+// bulk-synchronous snapshot.
+template <bool PR>
 __global__ void __launch_bounds__(kGenThreads) k_generate_write(GenArgs a) {
   __shared__ unsigned long long s_warp[kGenThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -661,7 +717,7 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_write(GenArgs a) {
   if (v0 < a.n) {
     const uint32_t gm = a.gmask[v0 / kGenVPerLane];
     L.keepmask = gm & 0xffffu;
-    if (a.edge_limit && (gm >> 16)) {  // the clearing the count pass left to this tile
+    if (!PR && a.edge_limit && (gm >> 16)) {  // the clearing the count pass left to this tile
       L.clearmask = gm >> 16;
       if (full) {
         const uint4 x = *reinterpret_cast<const uint4 *>(a.l1 + v0);
@@ -709,12 +765,23 @@ __global__ void __launch_bounds__(kGenThreads) k_generate_write(GenArgs a) {
 #pragma unroll
     for (uint32_t k = 0; k < kGenVPerLane; ++k) {
       if ((L.keepmask >> k) & 1u) {
+        const uint32_t d = L.o[k + 1] - L.o[k];
         a.queue[pos] = v0 + k;
         a.ptr[pos] = ep;
+        if (PR) a.qpush[pos] = a.damping * a.delta[v0 + k] / (double)d;
         ++pos;
-        ep += L.o[k + 1] - L.o[k];
+        ep += d;
       }
     }
+  }
+  if (PR && v0 < a.n) {  // residuals of every active vertex (queued or of degree 0) into the ranks
+    const uint32_t cm = a.gmask[v0 / kGenVPerLane] >> 16;
+#pragma unroll
+    for (uint32_t k = 0; k < kGenVPerLane; ++k)
+      if ((cm >> k) & 1u) {
+        a.pval[v0 + k] += a.delta[v0 + k];
+        a.delta[v0 + k] = 0.0;
+      }
   }
 }
 

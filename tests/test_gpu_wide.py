@@ -113,12 +113,34 @@ def test_generate_edge_limit(gpu, orc, wide, policy):
         e.close()
 
 
+@pytest.mark.parametrize("wide", [False, True])
+def test_pagerank_generate_edge_limit(gpu, orc, wide):
+    """PageRank's generate under an edge limit: tiles past the limit keep
+    their residuals for the next round.  Ranks stay within the residual bound
+    of the FP64 oracle (twice acc / init, both being within acc / init of the
+    fixpoint), and without a limit within 2.5e-7 (the same bulk-synchronous
+    rounds)."""
+    g = gpu.Graph.rmat(14, 16, seed=32)
+    if wide:
+        g = _wide(gpu, g)
+    init, acc, damp = (float(np.float32(x)) for x in (0.15, 1e-3, 0.85))
+    ref, _ = orc.pagerank(g.node_pointer, g.ends, init=init, acc=acc, damping=damp)
+    budget = 36 * g.n + 128 * 1024 + (g.m // 3) * 4 * 2
+    for lim, bound in ((0, 2.5e-7), (1, 2 * acc / init), (g.m // 4, 2 * acc / init)):
+        e = gpu.Engine(g, budget_bytes=budget, generate_edge_limit=lim)
+        for mode in MODES:
+            vals, st = e.run("pr", mode, pr_acc=acc)
+            rel = np.max(np.abs(vals.astype(np.float64) - ref) / ref)
+            assert rel < (bound if mode == "sync" else 2 * acc / init), (lim, mode, rel)
+        e.close()
+
+
 def test_graph_past_2pow32_edges(gpu, orc):
     """R-MAT scale 28, edge factor 17, unweighted: more than 2^32 edges, so
     the library keeps u64 node pointers, the engine gathers from host
     positions above 2^32 and limits each generate to 2^31 edges.  BFS (both
     modes, plain and learned schedules, 8 GB budget) equals the OpenMP
-    oracle; a u32 file refuses the graph; PageRank refuses it."""
+    oracle; a u32 file refuses the graph."""
     g = gpu.Graph.rmat(28, 17, seed=28)
     assert g.m >= 2 ** 32
     npt = g.node_pointer
@@ -132,8 +154,6 @@ def test_graph_past_2pow32_edges(gpu, orc):
         vals, st = eng.run("bfs", mode, 0)
         assert np.array_equal(vals, ref), (mode, int(np.count_nonzero(vals != ref)))
         assert st["reached_edges"] > 2 ** 32
-    with pytest.raises(gpu.SgwError):
-        eng.run("pr", "sync")
     eng.set_policy("learned")
     vals, _ = eng.run("bfs", "async", 0)
     assert np.array_equal(vals, ref)
