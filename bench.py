@@ -96,6 +96,9 @@ def parse_args(argv=None):
                     help="scale27: BFS, CC, SSWP (and PR with --suite-pr) sync and async on R-MAT scale 27 "
                          "under a 4 GB budget plus an Erdos-Renyi control, each checked against the oracle")
     ap.add_argument("--suite-pr", action="store_true", help="add PageRank (6 GB budget) to the suite")
+    ap.add_argument("--profile-engine", choices=["service", "one-query"], default="service",
+                    help="with --profile-run: the long-lived engine (pinned packed copy, the value's) or the "
+                         "one-query engine of the drop-in apps and of e2e (records read in place)")
     ap.add_argument("--profile-run", action="store_true",
                     help="one warm-up run and one measured run of --policy (plain or learned) from the first "
                          "two sources; prints each run's launches per kernel class (for ncu -s / -c) and the "
@@ -520,16 +523,19 @@ def run_profile(a, dist):
     g = N.Graph.rmat(a.scale, a.edge_factor, seed=a.seed, weighted=weighted, wmax=64)
     src = [int(s) for s in g.pick_sources(2, seed=a.seed)]
     nb = (a.num_buffers or N.sched_buffers(g, a.budget)) if policy == "learned" else 0
-    e = N.Engine(g, budget_bytes=int(a.budget), device=dist.local, flags=N.OPT_PROFILE, num_buffers=nb,
+    fl = N.OPT_PROFILE | ((N.OPT_GRAPH_IN_PLACE | N.OPT_PAGEABLE_COPY) if a.profile_engine == "one-query" else 0)
+    e = N.Engine(g, budget_bytes=int(a.budget), device=dist.local, flags=fl, num_buffers=nb,
                  gather_ctas=a.gather_ctas, tile_degree_max=a.tile_degree_max, chunk_edges=a.chunk_edges)
     if policy == "learned":
         e.set_policy("learned", scheduler.load_default(dist.local))
     out = np.empty(g.n, np.uint32)
     _, w = e.run(a.algo, a.mode, src[1], out=out)
     _, st = e.run(a.algo, a.mode, src[0], out=out)
-    esz = transfer_record_bytes(g.n, weighted, a.no_pack)
+    in_place = e.host_copy_bytes() == 0
+    esz = (8 if weighted else 4) if in_place else transfer_record_bytes(g.n, weighted, a.no_pack)
     keys = ("gather_launches", "relax_launches", "generate_launches", "launches")
-    return {"profile_run": policy, "workload": workload_config(a)["workload"],
+    return {"profile_run": policy, "engine": a.profile_engine, "records_in_place": in_place,
+            "workload": workload_config(a)["workload"],
             "warm": {k: w[k] for k in keys},
             "run": {k: st[k] for k in keys + ("ms_gather", "ms_relax", "ms_generate", "ms_device", "relaxed_edges",
                                               "relaxed_sources", "active_vertices", "gather_bytes", "h2d_bytes")},
