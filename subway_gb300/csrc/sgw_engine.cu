@@ -1986,7 +1986,7 @@ extern "C" int sgw_generate_noalloc(uint8_t *d_label1, uint8_t *d_label2,
   a.consume = consume ? 1 : 0;
   a.delta = a.pval = a.qpush = nullptr;
   a.acc = a.damping = 0.0;
-  k_generate<false><<<a.num_tiles, kGenThreads, 0, s>>>(a);
+  k_generate<<<a.num_tiles, kGenThreads, 0, s>>>(a);
   CK(cudaGetLastError());
   Ctl h;
   CK(cudaMemcpyAsync(&h, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));

@@ -157,7 +157,6 @@ void pack_into(const sgw_graph *g, uint32_t nb, uint32_t *p) {
   for (int64_t i = 0; i < (int64_t)g->m; ++i) p[i] = (ed[2 * size_t(i) + 1] << nb) | ed[2 * size_t(i)];
 }
 
-void copy_records(const sgw_graph *g, void *out) { copy_bytes(out, g->edges, size_t(g->m) * g->esz); }
 
 uint32_t max_weight(const sgw_graph *g) {
   if (!g->weighted || g->m == 0) return 0;
@@ -172,15 +171,6 @@ uint32_t max_weight(const sgw_graph *g) {
   for (int64_t i = 0; i < (int64_t)g->m; ++i) wmax = std::max(wmax, ed[2 * size_t(i) + 1]);
   if (cacheable) g->wmax_cache.store(wmax, std::memory_order_relaxed);
   return wmax;
-}
-
-void split_into(const sgw_graph *g, uint32_t *ends, uint8_t *w8) {
-  const uint32_t *ed = (const uint32_t *)g->edges;
-#pragma omp parallel for
-  for (int64_t i = 0; i < (int64_t)g->m; ++i) {
-    ends[i] = ed[2 * size_t(i)];
-    w8[i] = (uint8_t)ed[2 * size_t(i) + 1];
-  }
 }
 
 // The same transforms for edges [e0, e1), written from out[0] on (one chunk

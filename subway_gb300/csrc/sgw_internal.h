@@ -90,13 +90,8 @@ void copy_records_range(const sgw_graph *g, void *out, uint64_t e0, uint64_t e1)
 // Parallel memcpy in 64 MiB pieces.
 void copy_bytes(void *dst, const void *src, size_t bytes);
 void pack_into(const sgw_graph *g, uint32_t nbits, uint32_t *out);
-// Parallel copy of the edge records (m * esz bytes) into out.
-void copy_records(const sgw_graph *g, void *out);
 // Largest edge weight (0 for an unweighted graph).
 uint32_t max_weight(const sgw_graph *g);
-// Split transfer format: destinations as u32 into ends, weights (all below
-// 256) as u8 into w8.
-void split_into(const sgw_graph *g, uint32_t *ends, uint8_t *w8);
 
 // Device address of a scheduler model's BF16 weights, and its device.
 const void *mlp_device_weights(const sgw_mlp *m);

@@ -269,14 +269,9 @@ __device__ __forceinline__ bool selected(int algo, uint32_t v, uint32_t bin) {
 // 32 per round: a lane reads label1|label2 of its vertex, the warp ballots the
 // activeness, and only active lanes read their node pointers to get degrees.
 // Active vertices of degree 0 have nothing to relax: their labels are
-// cleared here and they are not queued.
-//
-// PR form (prePrefix PR overload, shared/subgraph_generator.cu:24-41):
-// active = delta > acc.  An active vertex moves its delta into its rank here
-// (value += delta, delta = 0, the first half of pr_kernel,
-// shared/gpu_kernels.cu:234-250) and its queue entry carries the push
-// damping * delta / outdeg, so every round is a bulk-synchronous snapshot.
-template <bool PR>
+// cleared here and they are not queued.  Integer algorithms; the engine uses
+// the count / scan / write form, this single-pass form serves the
+// allocation-free entry point.
 __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
   __shared__ uint32_t s_tile;
   __shared__ unsigned long long s_warp[kGenThreads / 32];
@@ -293,28 +288,15 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
 
   uint32_t deg[kGenRounds];
   uint32_t keepmask[kGenRounds];
-  double push[PR ? kGenRounds : 1];
   uint32_t wcount = 0, wedges = 0, seen = 0;
   uint32_t sel_bin = 0;
-  if (!PR && (a.sel_mode & 2)) sel_bin = a.ctl->sel_bin;
+  if (a.sel_mode & 2) sel_bin = a.ctl->sel_bin;
 #pragma unroll
   for (int r = 0; r < kGenRounds; ++r) {
     const uint32_t v = wbase + r * 32 + lane;
     bool act = false, defer = false;
     uint32_t d = 0;
-    if (PR) {
-      push[PR ? r : 0] = 0.0;
-      if (v < a.n) {
-        const double res = a.delta[v];
-        act = res > a.acc;
-        if (act) {
-          d = __ldg(&a.off[v + 1]) - __ldg(&a.off[v]);
-          a.pval[v] += res;
-          a.delta[v] = 0.0;
-          if (d) push[PR ? r : 0] = a.damping * res / (double)d;
-        }
-      }
-    } else if (v < a.n) {
+    if (v < a.n) {
       act = (a.l1[v] | a.l2[v]) != 0;
       if (act) {
         d = __ldg(&a.off[v + 1]) - __ldg(&a.off[v]);
@@ -374,7 +356,6 @@ __global__ void __launch_bounds__(kGenThreads) k_generate(GenArgs a) {
       const uint32_t pos = (uint32_t)(run >> 32) + __popc(keepmask[r] & lt);
       a.queue[pos] = wbase + r * 32 + lane;
       a.ptr[pos] = (uint32_t)(run & 0xffffffffull) + (incl - deg[r]);
-      if (PR) a.qpush[pos] = push[PR ? r : 0];
     }
     run += ((unsigned long long)__popc(keepmask[r]) << 32) | tot;
   }
