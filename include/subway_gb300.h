@@ -510,9 +510,7 @@ int sgw_batch_results(const sgw_batch *b, const uint32_t **results);
  * buffers through thrust, shared/subgraph_generator.cu:138-150).
  *
  * For callers that cannot call cudaMalloc: a host framework that already owns
- * every byte of device memory through its own pool, or a caller in a
- * latency-critical loop where cudaMalloc/cudaFree would synchronise the
- * device.  It runs the engine's activeness -> scan -> compaction kernel on
+ * every byte of device memory through its own pool.  It runs the engine's activeness -> scan -> compaction kernel on
  * device arrays the caller provides (label1, label2 bytes of n vertices;
  * node_pointer of n+1 entries; queue of n and ptr of n+1 entries), with the
  * scan's tile state in a static device array inside this library
@@ -522,12 +520,12 @@ int sgw_batch_results(const sgw_batch *b, const uint32_t **results);
  *  - consume != 0 clears the labels of queued vertices (the sync form);
  *    labels of active vertices with no out-edges are always cleared.
  *  - The first call on a device looks up the static array's device address
- *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture.
+ *    (cudaGetSymbolAddress) with that device current.
  *  - Every call shares the one static array: calls whose work overlaps on
  *    the GPU (other streams, other host threads) race; serialise them.
- *  - stream is a cudaStream_t (NULL = legacy default stream); the call
- *    synchronises it and returns the counts on the host. */
+ *  - stream is a cudaStream_t (NULL = legacy default stream); every call
+ *    synchronises it to return the counts on the host, so it cannot be
+ *    recorded into a stream capture or a CUDA graph. */
 #define SGW_NOALLOC_MAX_VERTICES 67108864u
 int sgw_generate_noalloc(uint8_t *d_label1, uint8_t *d_label2,
                          const uint32_t *d_node_pointer, uint32_t n, int consume,
