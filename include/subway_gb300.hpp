@@ -1,5 +1,5 @@
 // subway_gb300.hpp — C++ role classes over the C ABI, shaped like the
-// reference's Graph / Subgraph / SubgraphGenerator / Partitioner
+// reference's Graph / GraphPR / Subgraph / SubgraphGenerator / Partitioner
 // (shared/graph.cuh:7-59, shared/subgraph.cuh:8-29,
 // shared/subgraph_generator.cuh:12-30, shared/partitioner.cuh:8-22).
 //
@@ -67,6 +67,16 @@ class Graph {
   }
 };
 
+// GraphPR<E> (shared/graph.cuh:36-59): the same graph for PageRank.  Its
+// ranks and residuals live on the device (FP64; Subgraph::InitPR sets
+// value = 0 and delta = init, as subway/pr-sync.cu:33-40 does on the host)
+// and are read as float with Subgraph::ReadValues.
+template <class E>
+class GraphPR : public Graph<E> {
+ public:
+  GraphPR(std::string path, bool weighted) : Graph<E>(std::move(path), weighted) {}
+};
+
 template <class E>
 class Subgraph {
  public:
@@ -108,6 +118,23 @@ class Subgraph {
     (void)e;
   }
 
+  // PageRank's initial state (value = 0, delta = init) and first generate,
+  // with the activation threshold acc and the damping factor
+  // (subway/pr-sync.cu:33-34, shared/gpu_kernels.cu:239).
+  void InitPR(int mode, float init = 0.15f, float acc = 0.01f, float damping = 0.85f) {
+    sgw_run_params p;
+    sgw_run_params_default(&p, SGW_PR, mode, 0);
+    p.pr_init = init;
+    p.pr_acc = acc;
+    p.pr_damping = damping;
+    check(sgw_state_init(engine, &p), "InitPR");
+    uint32_t cnt = 0;
+    check(sgw_read_active(engine, nullptr, nullptr, 0xffffffffu, &cnt), "InitPR");
+    numActiveNodes = cnt;
+    pr_acc = acc;
+  }
+  float pr_acc = 0.01f;  // the threshold InitPR set
+
   template <class T>
   void ReadValues(std::vector<T> &out) {
     out.resize(num_nodes);
@@ -126,6 +153,13 @@ class SubgraphGenerator {
     check(sgw_generate(s.engine, &a, &e), "generate");
     s.numActiveNodes = a;
     s.numActiveEdges = e;
+  }
+  // The PageRank overload (shared/subgraph_generator.cu:128-204 with
+  // prePrefix's PR form, :24-41): acc is the threshold of the run, fixed by
+  // Subgraph::InitPR.
+  void generate(GraphPR<E> &g, Subgraph<E> &s, float acc) {
+    if (acc != s.pr_acc) throw Error(SGW_EINVAL, "generate: acc differs from the one InitPR set");
+    generate(static_cast<Graph<E> &>(g), s);
   }
 };
 
