@@ -33,6 +33,15 @@ def test_help_and_argument_errors_exit_zero(bindir, app):
     assert p.returncode == 0 and "error parsing command line argument <--bogus>" in p.stdout
 
 
+def test_extra_flags_in_help_and_parsed(bindir):
+    """--trace and --subway-compat are listed and parsed (a missing input file
+    then fails at the read, after parsing, with exit status 1)."""
+    p = _run(bindir, "bfs-async")
+    assert "[--trace]" in p.stdout and "[--subway-compat]" in p.stdout
+    p = _run(bindir, "bfs-async", "--input", "/nonexistent/g.bcsr", "--trace", "t.csv", "--subway-compat", "1")
+    assert "error parsing" not in p.stdout and p.returncode == 1 and "ReadGraph" in p.stderr
+
+
 def test_cc_sync_rejects_source(bindir):
     """cc-sync has no --source (subway/cc-sync.cu:17); cc-async accepts it."""
     p = _run(bindir, "cc-sync", "--input", "g.bcsr", "--source", "3")
